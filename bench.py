@@ -1,0 +1,410 @@
+"""Benchmark of the out-of-core tiled GEMM on GB300 (one JSON line on rank 0).
+
+Metric: FP64-accurate TFLOP/s (2 m n k / time) of the Ozaki emulated-FP64 path,
+reported beside the native FP64 (DMMA) path on the same inputs, with the
+componentwise error metric of both against a twice-working-precision oracle.
+
+Default workload (--workload ozaki32768): m = n = k = 32768, NN, entries u * 2^e
+with u uniform [-1, 1) and e a uniform integer in [-20, 20] (seeded, synthetic),
+alpha = 1, beta = 0, the slice count the smallest that meets the native path's
+error on a calibration sub-problem of the same k and distribution.
+  value    device-resident operands (tmm_gemm_device), CUDA-event timed
+  e2e      the public host-pointer call (tmm_gemm) with pinned host buffers:
+           every step copies A and B to the device and C back
+Other workloads: native4096 (m = n = k = 4096 NN, uniform, alpha = beta = 1,
+tiles 2048, 2 streams, pinned, copy_c_back).
+
+--impl reference times the reference algorithm's CPU restatement (the oracle;
+the reference itself is cuBLAS-backed GPU code that is not present on the GPU
+box) on the host cores, on a bounded k-slab of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "tiled-mm_gb300"))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+# measured on this machine's GB300 with the repository's own probes (mma.sync loops, CUDA events)
+MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 151.2, "dmma_f64_tflops": 1.054, "dfma_f64_tflops": 1.012}
+
+WORKLOADS = {
+    "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
+                       path="ozaki", tiles=(32768, 32768, 32768), streams=2,
+                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20]"),
+    "native4096": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=1.0, kind=0, param=0.0,
+                       path="native", tiles=(2048, 2048, 2048), streams=2,
+                       desc="FP64 GEMM m=n=k=4096 NN, uniform[-1,1), alpha=beta=1, tiles 2048, 2 streams"),
+}
+
+
+# ----------------------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.samples: list[list[str]] = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.samples.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) > 8:
+                for nm, v in zip(names, s[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus: int):
+    """torchrun ranks (one per GPU) or a single process."""
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch
+        import torch.distributed as dist
+
+        rank, world, local = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"]), int(os.environ["LOCAL_RANK"])
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        import torch
+
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peaks() -> dict:
+    try:
+        return json.loads(PEAKS_FILE.read_text())
+    except Exception:
+        return {}
+
+
+# ----------------------------------------------------------------------------- our implementation
+def error_metric_dev(tmm, w, a_h, b_h, c_out_h, nsamp=2048) -> float:
+    m, n, k = w["m"], w["n"], w["k"]
+    return tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, m if w["ta"] == "N" else k, b_h,
+                            k if w["tb"] == "N" else n, w["beta"], None, m, c_out_h, m, n_samples=nsamp, seed=7)
+
+
+def calibrate_slices(tmm, torch, w, native_metric_ref: float | None, log) -> tuple[int, dict]:
+    """Smallest slice count whose error metric meets the native path's on a sub-problem with the
+    workload's k and value distribution (m = n = 2048)."""
+    m = n = 2048
+    k = w["k"]
+    dev = torch.device("cuda")
+    a = torch.empty(m * k, dtype=torch.float64, device=dev)
+    b = torch.empty(k * n, dtype=torch.float64, device=dev)
+    tmm.fill_device(a.data_ptr(), m, k, m, w["kind"], w["param"], seed=101, mat_id=0)
+    tmm.fill_device(b.data_ptr(), k, n, k, w["kind"], w["param"], seed=101, mat_id=1)
+    a_h, b_h = a.cpu().numpy(), b.cpu().numpy()
+    ctx = tmm.make_context(np.float64, 1, 32768, 32768, 32768)
+    c = torch.zeros(m * n, dtype=torch.float64, device=dev)
+    tmm.gemm_device(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    sub = dict(w, m=m, n=n)
+    e_nat = error_metric_dev(tmm, sub, a_h, b_h, c.cpu().numpy())
+    sweep = {}
+    chosen = None
+    for s in range(6, 21):
+        ctx.set_path(tmm.PATH_OZAKI, s)
+        tmm.gemm_device(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m,
+                        stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        e = error_metric_dev(tmm, sub, a_h, b_h, c.cpu().numpy())
+        sweep[s] = e
+        log(f"calibration: slices={s} metric={e:.3e} (native {e_nat:.3e})")
+        if e <= e_nat:
+            chosen = s
+            break
+    ctx.close()
+    return (chosen or 20), {"native_metric": e_nat, "sweep": sweep, "m": m, "n": n, "k": k}
+
+
+def run_ours(args, w, rank, world, dist, log) -> dict:
+    import torch
+
+    import tiledmm as tmm
+
+    dev = torch.device("cuda")
+    m, n, k = w["m"], w["n"], w["k"]
+    lda = m if w["ta"] == "N" else k
+    ldb = k if w["tb"] == "N" else n
+    a_rows, a_cols = (m, k) if w["ta"] == "N" else (k, m)
+    b_rows, b_cols = (k, n) if w["tb"] == "N" else (n, k)
+    flops = 2.0 * m * n * k
+    stream = torch.cuda.current_stream()
+    sid = stream.cuda_stream
+    result: dict = {}
+
+    # ---- slice count
+    slices = None
+    calib = None
+    if w["path"] == "ozaki":
+        if args.slices:
+            slices = args.slices
+        else:
+            slices, calib = calibrate_slices(tmm, torch, w, None, log)
+        log(f"slices = {slices}")
+
+    # ---- device-resident operands
+    A = torch.empty(a_rows * a_cols, dtype=torch.float64, device=dev)
+    B = torch.empty(b_rows * b_cols, dtype=torch.float64, device=dev)
+    Cd = torch.empty(m * n, dtype=torch.float64, device=dev)
+    tmm.fill_device(A.data_ptr(), a_rows, a_cols, a_rows, w["kind"], w["param"], seed=rank, mat_id=0, stream=sid)
+    tmm.fill_device(B.data_ptr(), b_rows, b_cols, b_rows, w["kind"], w["param"], seed=rank, mat_id=1, stream=sid)
+    tmm.fill_device(Cd.data_ptr(), m, n, m, w["kind"], w["param"], seed=rank, mat_id=2, stream=sid)
+    C0 = Cd.clone()
+    ctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
+    if slices:
+        ctx.set_path(tmm.PATH_OZAKI, slices)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def dev_step():
+        tmm.gemm_device(ctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, m, stream=sid)
+
+    for _ in range(args.warmup):
+        Cd.copy_(C0)
+        dev_step()
+    torch.cuda.synchronize()
+    launches_per_step = ctx.stats()["kernels"]
+    # inputs (8.6 GB per operand at the default workload) are far larger than the 126 MB L2
+    times = []
+    barrier(dist)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            Cd.copy_(C0)  # restore C (also evicts L2); outside the event-timed region
+            ev[0].record(stream)
+            dev_step()
+            ev[1].record(stream)
+            ev[1].synchronize()
+            times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+    barrier(dist)
+    t_step = max_over_ranks(dist, float(np.mean(times)))
+    result["value"] = world * flops / t_step / 1e12
+    result["ms_per_step"] = t_step * 1e3
+    result["clocks"] = clk.summary()
+    result["gpu_launches"] = launches_per_step * args.steps
+
+    # ---- dominant kernel: per-launch time with CUDA events on its stream (one extra run)
+    # the gemm kernel of the engine is the dominant launch; its share comes from the ncu launch list
+    result["device_step_seconds"] = t_step
+
+    # ---- error metric of this path's result (sampled entries, compensated dot products on the host)
+    Cd.copy_(C0)
+    dev_step()
+    torch.cuda.synchronize()
+    a_h, b_h = A.cpu().numpy(), B.cpu().numpy()
+    c_out = Cd.cpu().numpy()
+    c0_h = C0.cpu().numpy() if w["beta"] != 0 else None
+    e_ours = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m, c_out, m,
+                              n_samples=args.samples, seed=11)
+    result["error_metric"] = e_ours
+
+    # ---- native path on the same device-resident inputs (for the "vs native" comparison)
+    if w["path"] == "ozaki" and not args.skip_native:
+        nctx = tmm.make_context(np.float64, 1, *w["tiles"])
+        Cd.copy_(C0)
+        ev[0].record(stream)
+        tmm.gemm_device(nctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, m, stream=sid)
+        ev[1].record(stream)
+        ev[1].synchronize()
+        t_nat = ev[0].elapsed_time(ev[1]) / 1e3
+        c_nat = Cd.cpu().numpy()
+        e_nat = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m, c_nat,
+                                 m, n_samples=args.samples, seed=11)
+        result["native"] = {"tflops": flops / t_nat / 1e12, "seconds": t_nat, "error_metric": e_nat,
+                            "kernel": "DMMA mma.sync m16n8k4 f64"}
+        nctx.close()
+    del C0
+    torch.cuda.empty_cache()
+
+    # ---- end to end through the public host-pointer call
+    pa = tmm.PinnedArray((a_rows * a_cols,))
+    pb = tmm.PinnedArray((b_rows * b_cols,))
+    pc = tmm.PinnedArray((m * n,))
+    pa.array[:] = a_h
+    pb.array[:] = b_h
+    del a_h, b_h, A, B, Cd
+    torch.cuda.empty_cache()
+    hctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
+    if slices:
+        hctx.set_path(tmm.PATH_OZAKI, slices)
+    e2e_times = []
+    for it in range(max(1, args.e2e_warmup) + args.e2e_steps):
+        pc.array[:] = 0.0
+        t0 = time.perf_counter()
+        tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], pa.array, lda, pb.array, ldb, w["beta"], pc.array, m,
+                 pin_host_buffers=False, copy_c_back=True)
+        t1 = time.perf_counter()
+        if it >= max(1, args.e2e_warmup):
+            e2e_times.append(t1 - t0)
+    st = hctx.stats()
+    t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
+    result["e2e"] = {"value": world * flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
+                     "d2h_bytes_per_step": st["d2h_bytes"], "seconds_per_step": t_e2e,
+                     "host_buffers": "pinned (cudaHostAlloc)", "steps": args.e2e_steps}
+    result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"]]
+    hctx.close()
+    ctx.close()
+    for p in (pa, pb, pc):
+        p.free()
+
+    eng = tmm.ozaki_engine()
+    if w["path"] == "ozaki":
+        pairs = slices * (slices + 1) // 2
+        lowp_ops = pairs * flops
+        peak = MEASURED_ENGINE_PEAKS["imma_s8_tops"] if eng["engine"] == "imma" else None
+        achieved = lowp_ops / t_step / 1e12
+        result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                              "frac": (achieved / peak) if peak else None, "traffic": None,
+                              "kernel": f"oz_gemm_{eng['engine']}", "ops": f"{pairs} slice-pair products x 2mnk",
+                              "peak_source": "measured on this pool's GB300 by the repository's mma.sync probe"}
+        result["slices"] = slices
+        result["slice_pairs"] = pairs
+        result["engine"] = eng
+        if calib:
+            result["calibration"] = calib
+    else:
+        peak = MEASURED_ENGINE_PEAKS["dmma_f64_tflops"]
+        result["roofline"] = {"bound": "tensor", "achieved": result["value"], "peak": peak, "unit": "TFLOP/s",
+                              "frac": result["value"] / peak, "traffic": None, "kernel": "gemm_f64_dmma",
+                              "peak_source": "measured on this pool's GB300 by the repository's mma.sync probe"}
+    return result
+
+
+def cpu_baseline(w, seconds_budget: float = 20.0) -> dict:
+    """The reference algorithm's CPU restatement (the oracle: tiled GEMM with the reference's tile
+    semantics, per-tile plain GEMM) on a k-slab of the workload, all host threads."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import load_oracle, oracle_gemm
+
+    import tiledmm as tmm
+
+    oracle = load_oracle()
+    cores = len(os.sched_getaffinity(0))
+    m, n = w["m"], w["n"]
+    k = 64
+    while True:
+        a = np.zeros(m * k)
+        b = np.zeros(k * n)
+        tmm.fill_host(a, m, k, m, w["kind"], w["param"], seed=0, mat_id=0)
+        tmm.fill_host(b, k, n, k, w["kind"], w["param"], seed=0, mat_id=1)
+        c = np.zeros(m * n)
+        t0 = time.perf_counter()
+        oracle_gemm(oracle, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m, (min(m, 4096), min(n, 4096), k),
+                    nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt * 4 > seconds_budget or k >= w["k"]:
+            break
+        k = min(w["k"], k * 4)
+    return {"value": 2.0 * m * n * k / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"k-slab m={m} n={n} k={k} of the workload ({dt:.1f} s)", "seconds": dt}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ozaki32768", choices=sorted(WORKLOADS))
+    ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--skip-native", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-warmup", type=int, default=1)
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank, world, local, dist = dist_setup(args.gpus)
+    log = (lambda s: print(s, file=sys.stderr, flush=True)) if rank == 0 else (lambda s: None)
+    config = {"workload": w["desc"], "m": w["m"], "n": w["n"], "k": w["k"], "trans": w["ta"] + w["tb"],
+              "alpha": w["alpha"], "beta": w["beta"], "path": w["path"], "parallelism": f"replicas{world}",
+              "l2": "inputs larger than L2 (C restored between steps)"}
+    base = {"metric": "FP64-accurate TFLOP/s (Ozaki emulated FP64 vs native DGEMM, same GB300 and error bound)",
+            "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded counter-based generator)", "config": config}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(w)
+        line = dict(base, impl="reference", value=cb["value"], ms_per_step=cb["seconds"] * 1e3,
+                    cpu_baseline=cb, e2e={"value": cb["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0})
+        line["config"] = dict(config, reference_note="the reference's per-tile arithmetic is cuBLAS on a GPU; "
+                              "its algorithm is timed here as the oracle's CPU restatement on the host cores")
+        print(json.dumps(line), flush=True)
+        return
+
+    res = run_ours(args, w, rank, world, dist, log)
+    if rank == 0:
+        line = dict(base)
+        line.update(res)
+        if not args.skip_cpu:
+            line["cpu_baseline"] = cpu_baseline(w)
+        peaks = measured_peaks()
+        if peaks:
+            line["measured_peaks_file"] = {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/*
+ * tmm_c_api.h — C ABI of the GB300 (sm_103a) out-of-core tiled GEMM.
+ *
+ * This is the drop-in boundary: plain pointers, sizes and status codes, no
+ * CUDA or C++ types in the signatures.  The C++ headers under
+ * include/Tiled-MM/ (the reference's public API: gpu::make_context,
+ * gpu::gemm, mm_handle::get_full_device_buffer_c, ...) are thin inline
+ * wrappers over these entry points, and any FFI (ctypes, cgo, JNI) can bind
+ * them directly.  Each entry point names the reference interface it replaces
+ * (file:line in eth-cscs/Tiled-MM).
+ *
+ * Semantics kept from the reference:
+ *   - C = alpha * op(A) * op(B) + beta * C, column-major, op in {N, T, C}
+ *     (lower case accepted: toupper, src/Tiled-MM/tiled_mm.cpp:503-504);
+ *   - host pointers; the call is synchronous (returns when C is final);
+ *   - beta == 0 never reads C (src/Tiled-MM/tiled_mm.cpp:325, 425);
+ *   - pin_host_buffers registers A, B (and C when copy_c_back || beta != 0)
+ *     for the call's duration (src/Tiled-MM/tiled_mm.cpp:529-554, 606-623);
+ *   - copy_c_back == 0 leaves the result on the device in a compact m x n
+ *     column-major buffer (ld = m) returned by tmm_get_full_c
+ *     (src/Tiled-MM/mm_handle.cpp:162-165, tests/test-multiply.cpp:339);
+ *   - device buffers grow and are never shrunk by a call
+ *     (src/Tiled-MM/device_vector.hpp:93-107);
+ *   - the tile-size policy of src/Tiled-MM/mm_handle.cpp:89-133 is the
+ *     default (TMM_TILE_POLICY_REFERENCE).
+ * Deliberate deviations (documented in the design doc):
+ *   - 64-bit sizes, leading dimensions and offsets (the reference's int
+ *     offsets overflow past 2^31 elements);
+ *   - invalid arguments are reported (the reference constructs but never
+ *     throws them, src/Tiled-MM/tiled_mm.cpp:516-527);
+ *   - stream synchronisation of this context's streams instead of a
+ *     device-wide cudaDeviceSynchronize (src/Tiled-MM/tiled_mm.cpp:602-604);
+ *   - an already-registered host buffer is used as is (and left registered).
+ */
+#ifndef TMM_C_API_H
+#define TMM_C_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tmm_context tmm_context;
+
+/* Scalar types of the reference's explicit instantiations
+ * (src/Tiled-MM/tiled_mm.cpp:626-668, src/Tiled-MM/mm_handle.cpp:167-170). */
+enum tmm_dtype {
+  TMM_FLOAT = 0,
+  TMM_DOUBLE = 1,
+  TMM_COMPLEX_FLOAT = 2, /* std::complex<float>: {re, im} pairs */
+  TMM_COMPLEX_DOUBLE = 3 /* std::complex<double> */
+};
+
+enum tmm_status {
+  TMM_SUCCESS = 0,
+  TMM_ERROR_INVALID_ARGUMENT = 1,
+  TMM_ERROR_CUDA = 2,
+  TMM_ERROR_OUT_OF_MEMORY = 3,
+  TMM_ERROR_NOT_SUPPORTED = 4,
+  TMM_ERROR_INTERNAL = 5,
+  TMM_ERROR_TIMEOUT = 6
+};
+
+/* Multiplication paths for TMM_DOUBLE. */
+enum tmm_path {
+  TMM_PATH_NATIVE = 0, /* FP64 tensor-core (DMMA) tile kernel */
+  TMM_PATH_OZAKI = 1   /* split-precision emulation on tcgen05 low-precision tensor cores */
+};
+
+/* Tile-size policies. */
+enum tmm_tile_policy {
+  TMM_TILE_POLICY_REFERENCE = 0, /* src/Tiled-MM/mm_handle.cpp:89-133 (divisor policy) */
+  TMM_TILE_POLICY_FIXED = 1,     /* use the context's max tile sizes, clipped to the matrix */
+  TMM_TILE_POLICY_AUTOTUNE = 2   /* the autotuner's choice per (dtype, path, size class) */
+};
+
+/* ------------------------------------------------------------------ context */
+
+/* Replaces gpu::make_context<Scalar>(streams, max_tile_m, max_tile_n, max_tile_k)
+ * (src/Tiled-MM/mm_handle.hpp:60-69) and mm_handle::mm_handle
+ * (src/Tiled-MM/mm_handle.cpp:11-29).  Creates the streams on the caller's
+ * current device; allocates no device memory (buffers are sized lazily by the
+ * first gemm, as in the reference). */
+int tmm_create(int dtype, int n_streams, int max_tile_m, int max_tile_n, int max_tile_k,
+               tmm_context** ctx);
+
+/* Replaces mm_handle::~mm_handle / gpu_context::~gpu_context
+ * (src/Tiled-MM/mm_handle.cpp:32-34, src/Tiled-MM/gpu_context.cpp:59-63). */
+int tmm_destroy(tmm_context* ctx);
+
+/* ------------------------------------------------------------------ GEMM */
+
+/* Replaces gpu::gemm<Scalar>(mm_handle&, trans_a, trans_b, m, n, k, alpha, a,
+ * ld_a, b, ld_b, beta, c, ld_c, pin_host_buffers, copy_c_back)
+ * (src/Tiled-MM/tiled_mm.hpp:69-79, src/Tiled-MM/tiled_mm.cpp:492-624).
+ * alpha and beta point to one scalar of the context's dtype. */
+int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
+             const void* alpha, const void* a, int64_t ld_a, const void* b, int64_t ld_b,
+             const void* beta, void* c, int64_t ld_c, int pin_host_buffers, int copy_c_back);
+
+/* Same product on operands already in device memory (no host copies), on the
+ * given CUDA stream (a cudaStream_t, or NULL for the context's first stream).
+ * Returns after the work is enqueued; the caller synchronises the stream.
+ * No reference counterpart: it is the device-pointer entry of the tile
+ * kernel that src/Tiled-MM/tiled_mm.cpp:200-217 reaches through cuBLAS. */
+int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
+                    const void* alpha, const void* a_dev, int64_t ld_a, const void* b_dev, int64_t ld_b,
+                    const void* beta, void* c_dev, int64_t ld_c, void* stream);
+
+/* Replaces mm_handle::get_full_device_buffer_c() (src/Tiled-MM/mm_handle.cpp:162-165)
+ * and its device_vector::data()/size()/capacity() (src/Tiled-MM/device_vector.hpp:67-80):
+ * the device pointer of the compact (ld = m) result left by copy_c_back == 0. */
+int tmm_get_full_c(tmm_context* ctx, void** device_ptr, size_t* size_elems, size_t* capacity_elems);
+
+/* ------------------------------------------------------------------ handle settings */
+
+/* mm_handle::set_num_streams / get_num_streams (src/Tiled-MM/mm_handle.cpp:37-50). */
+int tmm_set_num_streams(tmm_context* ctx, int n_streams);
+int tmm_get_num_streams(tmm_context* ctx, int* n_streams);
+
+/* mm_handle::set_tile_sizes (src/Tiled-MM/mm_handle.cpp:58-71): records the
+ * current tile sizes (and grows the tile buffers on next use). */
+int tmm_set_tile_sizes(tmm_context* ctx, int tile_m, int tile_n, int tile_k);
+/* device_buffer::get_tile_sizes of the C and A buffers (src/Tiled-MM/device_buffer.hpp:181-184):
+ * the tile sizes used by the last call (tile_m, tile_n from C; tile_k from A). */
+int tmm_get_tile_sizes(tmm_context* ctx, int* tile_m, int* tile_n, int* tile_k);
+
+/* mm_handle::set_full_sizes (src/Tiled-MM/mm_handle.cpp:74-80): grow the full-C buffer to m*n. */
+int tmm_set_full_sizes(tmm_context* ctx, int64_t m, int64_t n, int64_t k);
+
+/* mm_handle::optimal_tile_sizes (src/Tiled-MM/mm_handle.cpp:117-133). */
+int tmm_optimal_tile_sizes(tmm_context* ctx, int64_t m, int64_t n, int64_t k, int* tile_m, int* tile_n,
+                           int* tile_k);
+
+/* mm_handle::get_max_tile_sizes (src/Tiled-MM/mm_handle.cpp:112-115). */
+int tmm_get_max_tile_sizes(tmm_context* ctx, int* tile_m, int* tile_n, int* tile_k);
+
+/* mm_handle::set_streams_and_tiles (src/Tiled-MM/mm_handle.cpp:135-145). */
+int tmm_set_streams_and_tiles(tmm_context* ctx, int n_streams, int tile_m, int tile_n, int tile_k);
+
+/* New: multiplication path for TMM_DOUBLE contexts and the Ozaki slice count
+ * (slices <= 0 selects the default). */
+int tmm_set_path(tmm_context* ctx, int path, int ozaki_slices);
+int tmm_get_path(tmm_context* ctx, int* path, int* ozaki_slices);
+
+/* New: the engine behind TMM_PATH_OZAKI (0 = IMMA mma.sync int8, 1 = tcgen05 e4m3),
+ * its k-block (elements) and the k-blocks accumulated exactly between two FP64
+ * recombination steps. */
+int tmm_get_ozaki_engine(int* engine, int* k_block, int64_t* pass_blocks);
+
+/* New: tile policy (enum tmm_tile_policy). */
+int tmm_set_tile_policy(tmm_context* ctx, int policy);
+
+/* New: cap on the device memory the context may hold (0 = no cap beyond what
+ * is free on the device).  Smaller caps force out-of-core tiling. */
+int tmm_set_memory_limit(tmm_context* ctx, size_t bytes);
+
+/* ------------------------------------------------------------------ diagnostics */
+
+typedef struct tmm_stats {
+  uint64_t h2d_bytes;     /* host -> device bytes of the last call */
+  uint64_t d2h_bytes;     /* device -> host bytes of the last call */
+  uint64_t kernels;       /* kernel launches of the last call */
+  uint64_t tiles_loaded;  /* A/B tiles copied to the device */
+  uint64_t tiles_reused;  /* A/B tile uses served from device-resident tiles */
+  int tile_m, tile_n, tile_k, n_streams;
+  int path, ozaki_slices;
+  double seconds;         /* host wall time of the last call */
+} tmm_stats;
+
+int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);
+
+/* Message of the last failure of this context (ctx == NULL: of the calling
+ * thread's last context-free call).  Never NULL. */
+const char* tmm_last_error(tmm_context* ctx);
+const char* tmm_status_string(int status);
+
+/* ------------------------------------------------------------------ utilities */
+
+/* gpu::malloc_pinned (src/Tiled-MM/util.hpp:64-72): page-locked host memory. */
+int tmm_malloc_pinned(size_t bytes, void** ptr);
+int tmm_free_pinned(void* ptr);
+/* gpu::copy_to_device / copy_to_host (src/Tiled-MM/util.hpp:79-88). */
+int tmm_copy_to_device(const void* host, void* device, size_t bytes);
+int tmm_copy_to_host(const void* device, void* host, size_t bytes);
+/* gpu::copy_to_device_async / copy_to_host_async (src/Tiled-MM/util.hpp:90-118): direction
+ * inferred from the pointers (unified addressing); stream is a cudaStream_t or NULL. */
+int tmm_memcpy_async(void* dst, const void* src, size_t bytes, void* stream);
+/* gpu::malloc_device (src/Tiled-MM/util.hpp:56-62) and its release. */
+int tmm_malloc_device(size_t bytes, void** ptr);
+int tmm_free_device(void* ptr);
+
+/* Seeded synthetic matrices (kind: see tiled-mm_gb300/csrc/tmm_datagen.h).
+ * The host and device generators give identical values element by element. */
+int tmm_fill_host_f64(double* x, int64_t rows, int64_t cols, int64_t ld, int kind, double param,
+                      uint64_t seed, uint64_t id, int n_threads);
+int tmm_fill_device_f64(double* x, int64_t rows, int64_t cols, int64_t ld, int kind, double param,
+                        uint64_t seed, uint64_t id, void* stream);
+
+/* Componentwise error metric of a computed FP64 GEMM on sampled entries:
+ * max |C(i,j) - C*(i,j)| / (k * 2^-53 * (|alpha| |op(A)||op(B)| + |beta| |C0|)(i,j)),
+ * with C* evaluated in twice-working precision (compensated dot product).
+ * c0 is the input C (may be NULL when beta == 0), c the result. */
+int tmm_error_metric_f64(char trans_a, char trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                         const double* a, int64_t ld_a, const double* b, int64_t ld_b, double beta,
+                         const double* c0, int64_t ld_c0, const double* c, int64_t ld_c, int64_t n_samples,
+                         uint64_t seed, int n_threads, double* metric);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TMM_C_API_H */

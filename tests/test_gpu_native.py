@@ -1,0 +1,232 @@
+"""GPU parity of the native path (FP64 DMMA tile kernel, FP32/complex SIMT kernels) and of the
+out-of-core pipeline, through the C ABI, against the oracle and the reference's golden vectors."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gpu_helpers import dense, exact_product, make_problem, tol_for
+from oracle_lib import oracle_gemm, reference_tiles
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = np.load(Path(__file__).parent / "golden" / "reference_host_golden.npz")
+CASES = sorted({k.split("/")[0] for k in GOLDEN.files if "/" in k})
+
+
+def run(tmm, ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pin=True, copy_c_back=True):
+    tmm.gemm(ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pin, copy_c_back)
+    if copy_c_back:
+        return c
+    full = np.zeros(m * n, dtype=a.dtype)
+    ctx.get_full_device_buffer_c().to_host(full)
+    return full
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("copy_c_back", [True, False])
+def test_reference_golden_bit_exact(tmm, name, copy_c_back):
+    """The reference's own known-answer runs (integer inputs: every correct GEMM is bit-equal)."""
+    p = GOLDEN[f"{name}/params"]
+    m, n, k, ta, tb = int(p[0]), int(p[1]), int(p[2]), chr(p[3]), chr(p[4])
+    tm, tn, tk, streams = (int(x) for x in p[5:9])
+    lda, ldb, ldc = (int(x) for x in p[9:12])
+    ref_tiles = tuple(int(x) for x in p[12:15])
+    alpha, beta = (float(x) for x in GOLDEN[f"{name}/scalars"])
+    a = GOLDEN[f"{name}/a"].astype(np.float64)
+    b = GOLDEN[f"{name}/b"].astype(np.float64)
+    c = GOLDEN[f"{name}/c"].astype(np.float64)
+    ctx = tmm.make_context(np.float64, streams, tm, tn, tk)
+    out = run(tmm, ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c.copy(), ldc, True, copy_c_back)
+    assert ctx.get_tile_sizes() == ref_tiles  # same tile policy decision as the reference
+    exact = exact_product(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc)
+    if copy_c_back:
+        want = GOLDEN[f"{name}/c_copy_back"] if name != "tn_short_k_tile" else None
+        if want is not None:
+            np.testing.assert_array_equal(out, want)
+        np.testing.assert_array_equal(dense(out, ldc, m, n), exact)
+    else:
+        if ldc == m and name != "tn_short_k_tile":
+            np.testing.assert_array_equal(out, GOLDEN[f"{name}/full_c"])
+        np.testing.assert_array_equal(out.reshape(n, m).T, exact)
+
+
+DTYPES = [np.float32, np.float64, np.complex64, np.complex128]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("trans", ["NN", "NT", "TN", "TT", "CN", "NC", "CC"])
+@pytest.mark.parametrize("copy_c_back", [True, False])
+def test_all_types_and_transposes_vs_oracle(tmm, oracle, dtype, trans, copy_c_back):
+    rng = np.random.default_rng(hash((trans, np.dtype(dtype).str)) % 2**32)
+    m, n, k = 97, 75, 131
+    ta, tb = trans
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype, pad=0 if not copy_c_back else 5)
+    if np.dtype(dtype).kind == "c":
+        alpha, beta = dtype(0.5 - 1.25j), dtype(-0.75 + 0.5j)
+    else:
+        alpha, beta = dtype(1.5), dtype(-0.5)
+    ctx = tmm.make_context(dtype, 2, 48, 40, 64)
+    out = run(tmm, ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c.copy(), ldc, True, copy_c_back)
+    tiles = reference_tiles(oracle, m, n, k, (48, 40, 64))
+    assert ctx.get_tile_sizes() == tiles
+    cc = c.copy()
+    _, full = oracle_gemm(oracle, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, cc, ldc, tiles, copy_c_back)
+    want = cc if copy_c_back else full
+    scale = np.abs(want).max()
+    np.testing.assert_allclose(out, want, rtol=0, atol=tol_for(dtype, k) * max(scale, 1))
+
+
+def test_beta_zero_never_reads_c(tmm):
+    rng = np.random.default_rng(1)
+    m, n, k = 70, 90, 50
+    a, lda, b, ldb, _, ldc = make_problem(rng, "N", "N", m, n, k)
+    c = np.full(ldc * n, np.nan)
+    ctx = tmm.make_context(np.float64, 2, 32, 32, 32)
+    run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, c, ldc)
+    assert np.isfinite(c).all()
+    np.testing.assert_allclose(dense(c, ldc, m, n), exact_product("N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, c, ldc),
+                               rtol=1e-13, atol=1e-13)
+
+
+def test_lowercase_trans_and_k_zero(tmm):
+    rng = np.random.default_rng(2)
+    m, n = 20, 30
+    c = rng.uniform(-1, 1, m * n)
+    c0 = c.copy()
+    ctx = tmm.make_context(np.float64, 2, 16, 16, 16)
+    a = np.zeros(1)
+    tmm.gemm(ctx, "n", "t", m, n, 0, 1.0, a, m, a, n, 2.0, c, m)
+    np.testing.assert_array_equal(c, 2.0 * c0)  # k == 0: C = beta C
+
+
+def test_invalid_arguments_raise(tmm):
+    ctx = tmm.make_context(np.float64, 2, 16, 16, 16)
+    a = np.zeros(100)
+    with pytest.raises(RuntimeError, match="GPU ERROR"):
+        tmm.gemm(ctx, "X", "N", 4, 4, 4, 1.0, a, 4, a, 4, 0.0, a, 4)
+    with pytest.raises(RuntimeError, match="GPU ERROR"):
+        tmm.gemm(ctx, "N", "N", 4, 4, 4, 1.0, a, 3, a, 4, 0.0, a, 4)  # ld_a < m
+    with pytest.raises(RuntimeError, match="GPU ERROR"):
+        ctx.set_tile_sizes(17, 1, 1)  # above the context's maximum (mm_handle.cpp:58-61)
+
+
+@pytest.mark.parametrize("streams", [1, 2, 3, 5])
+def test_stream_count_does_not_change_results(tmm, streams):
+    rng = np.random.default_rng(3)
+    m, n, k = 300, 260, 200
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k)
+    ctx1 = tmm.make_context(np.float64, 1, 64, 64, 64)
+    ctxs = tmm.make_context(np.float64, streams, 64, 64, 64)
+    o1 = run(tmm, ctx1, "T", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
+    os_ = run(tmm, ctxs, "T", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
+    np.testing.assert_array_equal(o1, os_)
+
+
+def test_resident_operands_cross_the_link_once(tmm):
+    rng = np.random.default_rng(4)
+    m, n, k = 512, 384, 640
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k)
+    ctx = tmm.make_context(np.float64, 2, 128, 128, 128)
+    run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, c.copy(), ldc)
+    st = ctx.stats()
+    assert st["h2d_bytes"] == 8 * (m * k + k * n + m * n)  # compulsory traffic only
+    assert st["d2h_bytes"] == 8 * m * n
+    assert st["tiles_loaded"] == (m // 128) * (k // 128) + (k // 128) * (n // 128)
+
+
+def test_out_of_core_eviction_matches_in_core(tmm):
+    rng = np.random.default_rng(5)
+    m, n, k = 640, 512, 768
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k)
+    big = tmm.make_context(np.float64, 2, 128, 128, 128)
+    small = tmm.make_context(np.float64, 2, 128, 128, 128)
+    tile = 128 * 128 * 8
+    small.set_memory_limit(4 * 2 * tile + 12 * tile)  # C slots + a few A/B tiles: forces eviction
+    o1 = run(tmm, big, "N", "T", m, n, k, 1.0, a, lda, b, ldb, 1.0, c.copy(), ldc)
+    o2 = run(tmm, small, "N", "T", m, n, k, 1.0, a, lda, b, ldb, 1.0, c.copy(), ldc)
+    np.testing.assert_array_equal(o1, o2)
+    assert small.stats()["tiles_loaded"] > big.stats()["tiles_loaded"]
+
+
+def test_pinned_and_pageable_host_buffers(tmm):
+    rng = np.random.default_rng(6)
+    m, n, k = 200, 100, 150
+    pa = tmm.PinnedArray((m * k,))
+    pa.array[:] = rng.uniform(-1, 1, m * k)
+    b = rng.uniform(-1, 1, k * n)
+    c1, c2 = np.zeros(m * n), np.zeros(m * n)
+    ctx = tmm.make_context(np.float64, 2, 64, 64, 64)
+    run(tmm, ctx, "N", "N", m, n, k, 1.0, pa.array, m, b, k, 0.0, c1, m, pin=True)  # already registered: used as is
+    run(tmm, ctx, "N", "N", m, n, k, 1.0, pa.array.copy(), m, b, k, 0.0, c2, m, pin=False)  # pageable
+    np.testing.assert_array_equal(c1, c2)
+    pa.free()
+
+
+def test_repeated_calls_are_deterministic_and_buffers_grow_only(tmm):
+    rng = np.random.default_rng(7)
+    ctx = tmm.make_context(np.float64, 2, 256, 256, 256)
+    caps = []
+    outs = []
+    for (m, n, k) in [(300, 300, 300), (100, 100, 100), (300, 300, 300)]:
+        a, lda, b, ldb, c, ldc = make_problem(np.random.default_rng(m), "N", "N", m, n, k)
+        outs.append(run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, c, ldc, copy_c_back=False))
+        caps.append(ctx.get_full_device_buffer_c().capacity())
+    np.testing.assert_array_equal(outs[0], outs[2])
+    assert caps[1] == caps[0] == caps[2]  # never shrinks (device_vector.hpp:93-107)
+
+
+@pytest.mark.parametrize("shape", [(1000, 1000, 1000), (1234, 4567, 1357)])
+def test_ctest_shapes_vs_oracle(tmm, oracle, shape):
+    """tests/CMakeLists.txt:11-14 shapes (default context: 2 streams, tiles 5000), integer inputs."""
+    m, n, k = shape
+    rng = np.random.default_rng(8)
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind="int09")
+    ctx = tmm.make_context(np.float64)
+    out = run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, c.copy(), ldc)
+    tiles = reference_tiles(oracle, m, n, k, (5000, 5000, 5000))
+    cc = c.copy()
+    oracle_gemm(oracle, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, cc, ldc, tiles, nthreads=16)
+    np.testing.assert_array_equal(out, cc)
+
+
+def test_ctest_square_large_sampled(tmm):
+    """10000^3 (tests/CMakeLists.txt:12) with integer inputs: exact on sampled rows."""
+    m = n = k = 10000
+    rng = np.random.default_rng(9)
+    a = rng.integers(0, 10, m * k).astype(np.float64)
+    b = rng.integers(0, 10, k * n).astype(np.float64)
+    c = np.zeros(m * n)
+    ctx = tmm.make_context(np.float64)
+    tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)
+    rows = rng.integers(0, m, 16)
+    A = a.reshape(k, m).T[rows].astype(np.int64)
+    B = b.reshape(n, k).T.astype(np.int64)
+    want = (A @ B).astype(np.float64)
+    np.testing.assert_array_equal(c.reshape(n, m).T[rows], want)
+
+
+def test_device_entry_matches_host_entry(tmm):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(10)
+    m, n, k = 333, 222, 111
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k)
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    host = run(tmm, ctx, "N", "T", m, n, k, 0.5, a, lda, b, ldb, 2.0, c.copy(), ldc)
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    s = torch.cuda.current_stream()
+    tmm.gemm_device(ctx, "N", "T", m, n, k, 0.5, da, lda, db, ldb, 2.0, dc, ldc, stream=s.cuda_stream)
+    s.synchronize()
+    np.testing.assert_array_equal(dc.cpu().numpy(), host)
+
+
+def test_device_generator_matches_host(tmm):
+    torch = pytest.importorskip("torch")
+    rows, cols, ld = 257, 33, 300
+    for kind, param in [(0, 0.0), (1, 0.0), (2, 20.0), (5, 16.0)]:
+        h = np.zeros(ld * cols)
+        tmm.fill_host(h, rows, cols, ld, kind, param, seed=5, mat_id=1)
+        d = torch.zeros(ld * cols, dtype=torch.float64, device="cuda")
+        tmm.fill_device(d.data_ptr(), rows, cols, ld, kind, param, seed=5, mat_id=1)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(d.cpu().numpy(), h)

@@ -1,0 +1,123 @@
+"""GPU parity of the Ozaki (emulated-FP64) path through the C ABI: bit-exact against the oracle's
+restatement of the same algorithm, exact on integer inputs, and within the native path's
+componentwise error bound on real-valued inputs."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gpu_helpers import dense, exact_product, make_problem
+from oracle_lib import dd_entries, ozaki_oracle, reference_tiles
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = np.load(Path(__file__).parent / "golden" / "reference_host_golden.npz")
+
+
+def ozaki_ctx(tmm, slices, tiles=(4096, 4096, 4096), streams=2):
+    ctx = tmm.make_context(np.float64, streams, *tiles)
+    ctx.set_path(tmm.PATH_OZAKI, slices)
+    return ctx
+
+
+@pytest.mark.parametrize("trans", ["NN", "NT", "TN", "TT"])
+@pytest.mark.parametrize("shape,tiles", [((129, 77, 200), (4096, 4096, 4096)),
+                                         ((300, 260, 517), (128, 256, 128)),
+                                         ((64, 1, 33), (4096, 4096, 4096))])
+def test_bit_exact_vs_oracle(tmm, oracle, trans, shape, tiles):
+    m, n, k = shape
+    ta, tb = trans
+    eng = tmm.ozaki_engine()
+    rng = np.random.default_rng(abs(hash((trans, shape))) % 2**32)
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, pad=3, kind="uexp")
+    slices = 7
+    ctx = ozaki_ctx(tmm, slices, tiles)
+    out = c.copy()
+    tmm.gemm(ctx, ta, tb, m, n, k, 0.75, a, lda, b, ldb, -1.25, out, ldc)
+    tm, tn, tk = reference_tiles(oracle, m, n, k, tiles)
+    assert ctx.get_tile_sizes() == (tm, tn, tk)
+    want = ozaki_oracle(oracle, ta, tb, m, n, k, 0.75, a, lda, b, ldb, -1.25, c.copy(), ldc, slices, tk,
+                        eng["k_block"], eng["pass_blocks"])
+    np.testing.assert_array_equal(out, want)
+
+
+@pytest.mark.parametrize("name", ["ci_small_tiles", "ci_smaller_than_tile", "beta_one", "beta_alpha", "tn", "nt",
+                                  "tt", "default_tiles", "tn_short_k_tile"])
+def test_reference_known_answers_exact(tmm, name):
+    """Integer inputs are represented exactly by one slice: the emulated product is exact."""
+    p = GOLDEN[f"{name}/params"]
+    m, n, k, ta, tb = int(p[0]), int(p[1]), int(p[2]), chr(p[3]), chr(p[4])
+    tm, tn, tk, streams = (int(x) for x in p[5:9])
+    lda, ldb, ldc = (int(x) for x in p[9:12])
+    alpha, beta = (float(x) for x in GOLDEN[f"{name}/scalars"])
+    a = GOLDEN[f"{name}/a"].astype(np.float64)
+    b = GOLDEN[f"{name}/b"].astype(np.float64)
+    c = GOLDEN[f"{name}/c"].astype(np.float64)
+    ctx = ozaki_ctx(tmm, 3, (tm, tn, tk), streams)
+    out = c.copy()
+    tmm.gemm(ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, out, ldc)
+    np.testing.assert_array_equal(dense(out, ldc, m, n), exact_product(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta,
+                                                                         c, ldc))
+    if name != "tn_short_k_tile":
+        np.testing.assert_array_equal(out, GOLDEN[f"{name}/c_copy_back"])
+
+
+@pytest.mark.parametrize("kind", ["uniform", "uexp"])
+def test_error_within_native_bound(tmm, oracle, kind):
+    rng = np.random.default_rng(11)
+    m, n, k = 256, 192, 1024
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind=kind)
+    native = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    cn = c.copy()
+    tmm.gemm(native, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, cn, ldc)
+    ii, jj = np.repeat(np.arange(0, m, 7), len(range(0, n, 5))), np.tile(np.arange(0, n, 5), len(range(0, m, 7)))
+    ref, mag = dd_entries(oracle, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, None, ldc, ii, jj)
+
+    def metric(x):
+        v = dense(x, ldc, m, n)[ii, jj].copy()
+        return oracle.tmmo_error_metric(len(ii), v.ctypes.data, ref.ctypes.data, mag.ctypes.data, k)
+
+    e_native = metric(cn)
+    errs = {}
+    for s in (4, 8, 11, 13, 16):
+        ctx = ozaki_ctx(tmm, s)
+        co = c.copy()
+        tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, co, ldc)
+        errs[s] = metric(co)
+    assert errs[4] > errs[16]  # more slices, less error
+    assert errs[16] <= max(e_native, 1e-3)  # enough slices meet the native path's bound
+    assert e_native < 1.0
+
+
+def test_device_entry_matches_host_entry(tmm):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(12)
+    m, n, k = 200, 300, 400
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k, kind="uexp")
+    ctx = ozaki_ctx(tmm, 9, (4096, 4096, 4096))
+    host = c.copy()
+    tmm.gemm(ctx, "T", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, host, ldc)
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    s = torch.cuda.current_stream()
+    tmm.gemm_device(ctx, "T", "N", m, n, k, 1.0, da, lda, db, ldb, 0.5, dc, ldc, stream=s.cuda_stream)
+    s.synchronize()
+    np.testing.assert_array_equal(dc.cpu().numpy(), host)
+
+
+def test_out_of_core_ozaki_matches_in_core(tmm):
+    rng = np.random.default_rng(13)
+    m, n, k = 512, 384, 640
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind="uexp")
+    big = ozaki_ctx(tmm, 8, (128, 128, 128))
+    small = ozaki_ctx(tmm, 8, (128, 128, 128))
+    small.set_memory_limit(2 * 1024 * 1024)  # forces A/B tile eviction
+    o1, o2 = c.copy(), c.copy()
+    tmm.gemm(big, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, o1, ldc)
+    tmm.gemm(small, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, o2, ldc)
+    np.testing.assert_array_equal(o1, o2)
+
+
+def test_ozaki_needs_double(tmm):
+    ctx = tmm.make_context(np.float32, 2, 64, 64, 64)
+    with pytest.raises(RuntimeError, match="GPU ERROR"):
+        ctx.set_path(tmm.PATH_OZAKI, 8)

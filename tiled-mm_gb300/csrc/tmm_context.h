@@ -1,0 +1,94 @@
+// Internal state of a tmm_context (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/tmm_c_api.h"
+
+namespace tmm {
+
+// A device allocation that only grows (src/Tiled-MM/device_vector.hpp:93-107:
+// capacity 1.2x the requested size when it has to grow).
+struct GrowBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;     // requested size
+  size_t capacity = 0;  // allocated size
+  cudaError_t reserve(size_t want);
+  void release();
+};
+
+// One device-resident A or B tile (raw FP64/FP32/complex, or Ozaki digit planes).
+struct Slot {
+  char* ptr = nullptr;
+  cudaEvent_t ready = nullptr;     // recorded when the tile's data is in place
+  cudaEvent_t last_use = nullptr;  // recorded after the last kernel that read it
+  int64_t key = -1;
+  uint64_t stamp = 0;
+  bool used = false;               // last_use has been recorded
+};
+
+struct TileCache {
+  std::vector<Slot> slots;
+  std::unordered_map<int64_t, int> index;
+  uint64_t clock = 0;
+  void invalidate() {
+    index.clear();
+    for (auto& s : slots) { s.key = -1; s.used = false; }
+  }
+  // slot holding key, or -1
+  int find(int64_t key) {
+    auto it = index.find(key);
+    return it == index.end() ? -1 : it->second;
+  }
+  // least recently used slot (free slots first)
+  int victim() {
+    int best = -1;
+    for (int i = 0; i < (int)slots.size(); ++i) {
+      if (slots[i].key < 0) return i;
+      if (best < 0 || slots[i].stamp < slots[best].stamp) best = i;
+    }
+    return best;
+  }
+};
+
+struct CSlot {
+  char* ptr = nullptr;
+  cudaEvent_t done = nullptr;  // the slot's previous tile has left for the host
+  bool used = false;
+};
+
+struct OzakiState;  // defined with the Ozaki engine
+
+}  // namespace tmm
+
+struct tmm_context {
+  int dtype = TMM_DOUBLE;
+  int device = 0;
+  int n_streams = 2;
+  int max_tile_m = 5000, max_tile_n = 5000, max_tile_k = 5000;
+  int cur_tile_m = 0, cur_tile_n = 0, cur_tile_k = 0;  // tile sizes of the last call (0 = none yet)
+  int path = TMM_PATH_NATIVE;
+  int ozaki_slices = 0;
+  int tile_policy = TMM_TILE_POLICY_REFERENCE;
+  size_t memory_limit = 0;
+
+  std::vector<cudaStream_t> streams;  // compute streams
+  cudaStream_t h2d = nullptr;         // host -> device copies
+  cudaStream_t prep = nullptr;        // tile preparation kernels (Ozaki split)
+  cudaStream_t d2h = nullptr;         // result stream (src/Tiled-MM/gpu_context.hpp:39)
+
+  tmm::GrowBuffer pool_a, pool_b, pool_c, full_c, staging, scratch;
+  tmm::TileCache cache_a, cache_b;
+  std::vector<tmm::CSlot> cslots;  // 2 per stream
+  std::vector<cudaEvent_t> staging_free;
+  size_t full_c_elems = 0;
+
+  tmm::OzakiState* oz = nullptr;
+
+  tmm_stats stats{};
+  std::string last_error;
+};

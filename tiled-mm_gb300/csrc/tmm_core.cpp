@@ -1,0 +1,927 @@
+// Host side of the C ABI: context, tile policy, tile cache and the
+// C-stationary stream pipeline that replaces the reference's round-robin
+// schedules (src/Tiled-MM/tiled_mm.cpp:270-454) and driver
+// (src/Tiled-MM/tiled_mm.cpp:492-624).
+//
+// Schedule.  C tiles are visited row panel by row panel (the reference's
+// row-major tile order, tiled_mm.cpp:300-301), with the column order
+// reversed on every other panel so the B tiles used last are used first
+// again.  A C tile stays on one compute stream for its whole k loop (beta on
+// k-tile 0, 1 afterwards: tiled_mm.cpp:309, 402).  A and B tiles live in two
+// device tile caches (LRU); a tile is copied to the device once and reused
+// by every C tile that needs it while it stays resident, so with enough HBM
+// each operand crosses the host link exactly once (the reference re-sends A
+// n_tiles_n times and B n_tiles_m times).  Copies run on their own stream and
+// are ordered against compute with events only; each compute stream owns two
+// C tile slots, so the copy-back of one tile overlaps the next tile's k loop.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+
+#include "tmm_context.h"
+#include "tmm_kernels.h"
+#include "tmm_ozaki.h"
+#include "tmm_datagen.h"
+
+using tmm::Op;
+
+namespace {
+
+thread_local std::string g_last_error = "no error";
+
+int fail(tmm_context* ctx, int status, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_fail(tmm_context* ctx, cudaError_t e, const char* what) {
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(ctx, e == cudaErrorMemoryAllocation ? TMM_ERROR_OUT_OF_MEMORY : TMM_ERROR_CUDA, msg);
+}
+
+#define TMM_CUDA(ctx, call)                                        \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);     \
+  } while (0)
+
+size_t elem_size(int dtype) {
+  switch (dtype) {
+    case TMM_FLOAT: return 4;
+    case TMM_DOUBLE: return 8;
+    case TMM_COMPLEX_FLOAT: return 8;
+    default: return 16;
+  }
+}
+
+bool is_zero(int dtype, const void* v) {
+  switch (dtype) {
+    case TMM_FLOAT: return *(const float*)v == 0.f;
+    case TMM_DOUBLE: return *(const double*)v == 0.0;
+    case TMM_COMPLEX_FLOAT: return ((const float*)v)[0] == 0.f && ((const float*)v)[1] == 0.f;
+    default: return ((const double*)v)[0] == 0.0 && ((const double*)v)[1] == 0.0;
+  }
+}
+
+int upper(char c) { return (c >= 'a' && c <= 'z') ? c - 32 : c; }
+
+bool parse_op(char c, int dtype, Op* op) {
+  switch (upper(c)) {
+    case 'N': *op = tmm::OP_N; return true;
+    case 'T': *op = tmm::OP_T; return true;
+    case 'C': *op = (dtype == TMM_COMPLEX_FLOAT || dtype == TMM_COMPLEX_DOUBLE) ? tmm::OP_C : tmm::OP_T; return true;
+    default: return false;
+  }
+}
+
+// The reference's tile policy (src/Tiled-MM/mm_handle.cpp:89-110).
+int optimal_tile_size(int64_t dim, int curr, int max_tile) {
+  if (curr < max_tile && dim <= max_tile) return (int)dim;
+  int64_t limit = std::min<int64_t>(max_tile, dim);
+  int64_t tile = 1;
+  for (int64_t i = 1; i <= limit; ++i)
+    if (dim % i == 0) tile = i;
+  if (std::llabs((int64_t)max_tile - tile) <= max_tile / 2) return (int)tile;
+  return (int)limit;
+}
+
+// restores the caller's current device on scope exit
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    else prev = -1;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int launch_tile_gemm(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
+                     const void* A, int64_t lda, const void* B, int64_t ldb, const void* beta, void* C,
+                     int64_t ldc, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  switch (ctx->dtype) {
+    case TMM_FLOAT:
+      e = k == 0 ? tmm::launch_scale_f32(m, n, *(const float*)beta, (float*)C, ldc, s)
+                 : tmm::launch_gemm_f32(opa, opb, m, n, k, *(const float*)alpha, (const float*)A, lda,
+                                        (const float*)B, ldb, *(const float*)beta, (float*)C, ldc, s);
+      break;
+    case TMM_DOUBLE:
+      e = k == 0 ? tmm::launch_scale_f64(m, n, *(const double*)beta, (double*)C, ldc, s)
+                 : tmm::launch_gemm_f64(opa, opb, m, n, k, *(const double*)alpha, (const double*)A, lda,
+                                        (const double*)B, ldb, *(const double*)beta, (double*)C, ldc, s);
+      break;
+    case TMM_COMPLEX_FLOAT:
+      e = k == 0 ? tmm::launch_scale_c32(m, n, *(const tmm::cplxf*)beta, (tmm::cplxf*)C, ldc, s)
+                 : tmm::launch_gemm_c32(opa, opb, m, n, k, *(const tmm::cplxf*)alpha, (const tmm::cplxf*)A, lda,
+                                        (const tmm::cplxf*)B, ldb, *(const tmm::cplxf*)beta, (tmm::cplxf*)C, ldc, s);
+      break;
+    default:
+      e = k == 0 ? tmm::launch_scale_c64(m, n, *(const tmm::cplxd*)beta, (tmm::cplxd*)C, ldc, s)
+                 : tmm::launch_gemm_c64(opa, opb, m, n, k, *(const tmm::cplxd*)alpha, (const tmm::cplxd*)A, lda,
+                                        (const tmm::cplxd*)B, ldb, *(const tmm::cplxd*)beta, (tmm::cplxd*)C, ldc, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "tile kernel launch");
+  ctx->stats.kernels++;
+  return TMM_SUCCESS;
+}
+
+int make_events(tmm_context* ctx, tmm::TileCache& c) {
+  for (auto& s : c.slots) {
+    if (!s.ready) TMM_CUDA(ctx, cudaEventCreateWithFlags(&s.ready, cudaEventDisableTiming));
+    if (!s.last_use) TMM_CUDA(ctx, cudaEventCreateWithFlags(&s.last_use, cudaEventDisableTiming));
+  }
+  return TMM_SUCCESS;
+}
+
+void destroy_events(tmm::TileCache& c) {
+  for (auto& s : c.slots) {
+    if (s.ready) cudaEventDestroy(s.ready);
+    if (s.last_use) cudaEventDestroy(s.last_use);
+    s.ready = s.last_use = nullptr;
+  }
+}
+
+// Host-range registration for one call (src/Tiled-MM/tiled_mm.cpp:529-554).
+// Registers exactly the bytes the matrix spans: ld*(cols-1)+rows elements.
+struct Pin {
+  void* ptr = nullptr;
+  bool owned = false;
+};
+
+int pin_range(tmm_context* ctx, const void* p, size_t bytes, Pin* out) {
+  out->ptr = nullptr;
+  out->owned = false;
+  if (!p || bytes == 0) return TMM_SUCCESS;
+  cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
+  if (e == cudaSuccess) {
+    out->ptr = const_cast<void*>(p);
+    out->owned = true;
+    return TMM_SUCCESS;
+  }
+  cudaGetLastError();  // clear the sticky-free error state of the failed call
+  if (e == cudaErrorHostMemoryAlreadyRegistered) return TMM_SUCCESS;
+  return cuda_fail(ctx, e, "cudaHostRegister");
+}
+
+void unpin(Pin& p) {
+  if (p.owned) cudaHostUnregister(p.ptr);
+  p.owned = false;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ GrowBuffer
+cudaError_t tmm::GrowBuffer::reserve(size_t want) {
+  if (want <= capacity) {
+    bytes = want;
+    return cudaSuccess;
+  }
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  capacity = 0;
+  size_t cap = (size_t)std::ceil(1.2 * (double)want);
+  cap = (cap + 255) / 256 * 256;
+  cudaError_t e = cudaMalloc(&ptr, cap);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&ptr, want);  // no headroom left: exact size
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      ptr = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+    cap = want;
+  }
+  capacity = cap;
+  bytes = want;
+  return cudaSuccess;
+}
+
+void tmm::GrowBuffer::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = capacity = 0;
+}
+
+// ------------------------------------------------------------------ C ABI: context
+extern "C" int tmm_create(int dtype, int n_streams, int max_tile_m, int max_tile_n, int max_tile_k,
+                          tmm_context** out) {
+  if (!out) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_create: null output");
+  *out = nullptr;
+  if (dtype < TMM_FLOAT || dtype > TMM_COMPLEX_DOUBLE)
+    return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_create: unknown dtype");
+  if (n_streams < 1 || max_tile_m < 1 || max_tile_n < 1 || max_tile_k < 1)
+    return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_create: streams and tile sizes must be positive");
+  auto* ctx = new tmm_context();
+  ctx->dtype = dtype;
+  ctx->n_streams = n_streams;
+  ctx->max_tile_m = max_tile_m;
+  ctx->max_tile_n = max_tile_n;
+  ctx->max_tile_k = max_tile_k;
+  cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->prep, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking);
+  for (int i = 0; e == cudaSuccess && i < n_streams; ++i) {
+    cudaStream_t s;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) ctx->streams.push_back(s);
+  }
+  if (e != cudaSuccess) {
+    int st = cuda_fail(nullptr, e, "tmm_create");
+    tmm_destroy(ctx);
+    return st;
+  }
+  *out = ctx;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_destroy(tmm_context* ctx) {
+  if (!ctx) return TMM_SUCCESS;
+  DeviceGuard dg(ctx->device);
+  for (auto s : ctx->streams) cudaStreamSynchronize(s);
+  if (ctx->h2d) cudaStreamSynchronize(ctx->h2d);
+  if (ctx->prep) cudaStreamSynchronize(ctx->prep);
+  if (ctx->d2h) cudaStreamSynchronize(ctx->d2h);
+  destroy_events(ctx->cache_a);
+  destroy_events(ctx->cache_b);
+  for (auto& c : ctx->cslots)
+    if (c.done) cudaEventDestroy(c.done);
+  for (auto e : ctx->staging_free)
+    if (e) cudaEventDestroy(e);
+  ctx->pool_a.release();
+  ctx->pool_b.release();
+  ctx->pool_c.release();
+  ctx->full_c.release();
+  ctx->staging.release();
+  ctx->scratch.release();
+  for (auto s : ctx->streams) cudaStreamDestroy(s);
+  if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
+  if (ctx->prep) cudaStreamDestroy(ctx->prep);
+  if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
+  delete ctx;
+  return TMM_SUCCESS;
+}
+
+// ------------------------------------------------------------------ settings
+extern "C" int tmm_set_num_streams(tmm_context* ctx, int n) {
+  if (!ctx || n < 1) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_num_streams: need n >= 1");
+  DeviceGuard dg(ctx->device);
+  while ((int)ctx->streams.size() < n) {
+    cudaStream_t s;
+    TMM_CUDA(ctx, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    ctx->streams.push_back(s);
+  }
+  ctx->n_streams = n;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_num_streams(tmm_context* ctx, int* n) {
+  if (!ctx || !n) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_num_streams: null argument");
+  *n = ctx->n_streams;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_tile_sizes(tmm_context* ctx, int tm, int tn, int tk) {
+  if (!ctx || tm < 1 || tn < 1 || tk < 1) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_tile_sizes: need positive sizes");
+  // src/Tiled-MM/mm_handle.cpp:58-66 asserts tile <= max tile
+  if (tm > ctx->max_tile_m || tn > ctx->max_tile_n || tk > ctx->max_tile_k)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_tile_sizes: tile larger than the context's maximum");
+  ctx->cur_tile_m = tm;
+  ctx->cur_tile_n = tn;
+  ctx->cur_tile_k = tk;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_tile_sizes(tmm_context* ctx, int* tm, int* tn, int* tk) {
+  if (!ctx || !tm || !tn || !tk) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_tile_sizes: null argument");
+  *tm = ctx->cur_tile_m;
+  *tn = ctx->cur_tile_n;
+  *tk = ctx->cur_tile_k;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_full_sizes(tmm_context* ctx, int64_t m, int64_t n, int64_t k) {
+  if (!ctx || m <= 0 || n <= 0 || k <= 0) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_full_sizes: need positive sizes");
+  DeviceGuard dg(ctx->device);
+  TMM_CUDA(ctx, ctx->full_c.reserve((size_t)m * (size_t)n * elem_size(ctx->dtype)));
+  ctx->full_c_elems = (size_t)m * (size_t)n;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_optimal_tile_sizes(tmm_context* ctx, int64_t m, int64_t n, int64_t k, int* tm, int* tn, int* tk) {
+  if (!ctx || !tm || !tn || !tk) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_optimal_tile_sizes: null argument");
+  *tm = optimal_tile_size(m, ctx->cur_tile_m, ctx->max_tile_m);
+  *tn = optimal_tile_size(n, ctx->cur_tile_n, ctx->max_tile_n);
+  *tk = optimal_tile_size(k, ctx->cur_tile_k, ctx->max_tile_k);
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_max_tile_sizes(tmm_context* ctx, int* tm, int* tn, int* tk) {
+  if (!ctx || !tm || !tn || !tk) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_max_tile_sizes: null argument");
+  *tm = ctx->max_tile_m;
+  *tn = ctx->max_tile_n;
+  *tk = ctx->max_tile_k;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_streams_and_tiles(tmm_context* ctx, int n_streams, int tm, int tn, int tk) {
+  int st = tmm_set_num_streams(ctx, n_streams);
+  if (st != TMM_SUCCESS) return st;
+  return tmm_set_tile_sizes(ctx, tm, tn, tk);
+}
+
+extern "C" int tmm_set_path(tmm_context* ctx, int path, int slices) {
+  if (!ctx) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: null context");
+  if (path != TMM_PATH_NATIVE && path != TMM_PATH_OZAKI)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: unknown path");
+  if (path == TMM_PATH_OZAKI && ctx->dtype != TMM_DOUBLE)
+    return fail(ctx, TMM_ERROR_NOT_SUPPORTED, "tmm_set_path: the Ozaki path emulates FP64 and needs a double context");
+  if (slices > tmm::OZ_MAX_SLICES)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: too many slices");
+  ctx->path = path;
+  ctx->ozaki_slices = slices > 0 ? slices : tmm::OZ_DEFAULT_SLICES;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_path(tmm_context* ctx, int* path, int* slices) {
+  if (!ctx || !path || !slices) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_path: null argument");
+  *path = ctx->path;
+  *slices = ctx->path == TMM_PATH_OZAKI ? ctx->ozaki_slices : 0;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_ozaki_engine(int* engine, int* k_block, int64_t* pass_blocks) {
+  if (!engine || !k_block || !pass_blocks) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_ozaki_engine: null argument");
+  *engine = tmm::ozaki_engine();
+  *k_block = (int)tmm::ozaki_k_block();
+  *pass_blocks = tmm::ozaki_pass_blocks();
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_tile_policy(tmm_context* ctx, int policy) {
+  if (!ctx || policy < TMM_TILE_POLICY_REFERENCE || policy > TMM_TILE_POLICY_AUTOTUNE)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_tile_policy: unknown policy");
+  ctx->tile_policy = policy;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_memory_limit(tmm_context* ctx, size_t bytes) {
+  if (!ctx) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_memory_limit: null context");
+  ctx->memory_limit = bytes;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_stats(tmm_context* ctx, tmm_stats* st) {
+  if (!ctx || !st) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_stats: null argument");
+  *st = ctx->stats;
+  return TMM_SUCCESS;
+}
+
+extern "C" const char* tmm_last_error(tmm_context* ctx) {
+  return ctx ? ctx->last_error.c_str() : g_last_error.c_str();
+}
+
+extern "C" const char* tmm_status_string(int status) {
+  switch (status) {
+    case TMM_SUCCESS: return "success";
+    case TMM_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case TMM_ERROR_CUDA: return "CUDA error";
+    case TMM_ERROR_OUT_OF_MEMORY: return "out of device memory";
+    case TMM_ERROR_NOT_SUPPORTED: return "not supported";
+    case TMM_ERROR_TIMEOUT: return "device wait timed out";
+    default: return "internal error";
+  }
+}
+
+extern "C" int tmm_get_full_c(tmm_context* ctx, void** ptr, size_t* size, size_t* capacity) {
+  if (!ctx || !ptr) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_full_c: null argument");
+  *ptr = ctx->full_c.ptr;
+  if (size) *size = ctx->full_c_elems;
+  if (capacity) *capacity = ctx->full_c.capacity / elem_size(ctx->dtype);
+  return TMM_SUCCESS;
+}
+
+// ------------------------------------------------------------------ the pipeline
+namespace {
+
+struct Plan {
+  int64_t m, n, k, tm, tn, tk;
+  int64_t ntm, ntn, ntk;
+  Op opa, opb;
+  size_t es;
+  bool ozaki;
+  int slices;
+  size_t a_slot_bytes, b_slot_bytes, c_slot_bytes, staging_bytes;
+};
+
+int64_t ntiles(int64_t len, int64_t t) { return len == 0 ? 0 : (len + t - 1) / t; }
+int64_t extent(int64_t len, int64_t t, int64_t id) { return std::min(t, len - id * t); }
+
+// Size the tile caches: everything resident when it fits, else one A row
+// panel (double-buffered when possible) and the rest for B.
+int plan_memory(tmm_context* ctx, const Plan& P, bool copy_back, size_t* n_a, size_t* n_b) {
+  size_t freeb = 0, total = 0;
+  TMM_CUDA(ctx, cudaMemGetInfo(&freeb, &total));
+  size_t held = ctx->pool_a.capacity + ctx->pool_b.capacity + ctx->pool_c.capacity + ctx->staging.capacity;
+  size_t avail = (size_t)((double)(freeb + held) * 0.92);
+  if (ctx->memory_limit) avail = std::min(avail, ctx->memory_limit);
+  size_t fixed = 0;
+  if (copy_back) fixed += 2 * (size_t)ctx->n_streams * P.c_slot_bytes;
+  else fixed += (size_t)P.m * (size_t)P.n * P.es;  // full C (held outside the cache budget)
+  fixed += 3 * P.staging_bytes;
+  if (avail <= fixed) return fail(ctx, TMM_ERROR_OUT_OF_MEMORY, "not enough device memory for the C tiles");
+  size_t budget = avail - fixed;
+  size_t total_a = (size_t)(P.ntm * P.ntk), total_b = (size_t)(P.ntk * P.ntn);
+  if (total_a * P.a_slot_bytes + total_b * P.b_slot_bytes <= budget) {
+    *n_a = total_a;
+    *n_b = total_b;
+    return TMM_SUCCESS;
+  }
+  // A: one panel (+ one panel of prefetch when it fits), at least 2 slots
+  size_t want_a = std::min(total_a, (size_t)(2 * P.ntk));
+  while (want_a > 2 && want_a * P.a_slot_bytes + 2 * P.b_slot_bytes > budget) --want_a;
+  if (want_a < 2) want_a = std::min<size_t>(2, total_a);
+  if (want_a * P.a_slot_bytes + std::min<size_t>(2, total_b) * P.b_slot_bytes > budget)
+    return fail(ctx, TMM_ERROR_OUT_OF_MEMORY, "not enough device memory for two A and two B tiles");
+  size_t want_b = std::min(total_b, (budget - want_a * P.a_slot_bytes) / P.b_slot_bytes);
+  *n_a = want_a;
+  *n_b = std::max<size_t>(want_b, std::min<size_t>(2, total_b));
+  return TMM_SUCCESS;
+}
+
+int setup_cache(tmm_context* ctx, tmm::TileCache& c, tmm::GrowBuffer& pool, size_t n, size_t slot_bytes) {
+  const size_t sb = (slot_bytes + 255) / 256 * 256;
+  TMM_CUDA(ctx, pool.reserve(n * sb));
+  while (c.slots.size() > n) {  // drop surplus slots (no work is pending: every call ends synchronised)
+    tmm::Slot& s = c.slots.back();
+    if (s.ready) cudaEventDestroy(s.ready);
+    if (s.last_use) cudaEventDestroy(s.last_use);
+    c.slots.pop_back();
+  }
+  c.slots.resize(n);
+  for (size_t i = 0; i < n; ++i) c.slots[i].ptr = (char*)pool.ptr + i * sb;
+  int st = make_events(ctx, c);
+  if (st) return st;
+  c.invalidate();
+  return TMM_SUCCESS;
+}
+
+struct HostMat {
+  const char* ptr;
+  int64_t ld;  // elements
+};
+
+// Brings tile `key` (stored sub-block rows r0.., cols c0.. of size rr x cc)
+// into the cache; returns the slot.  The copy waits for the evicted tile's
+// last reader.  Ozaki tiles are staged raw, then split on the prep stream.
+int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t key, const HostMat& h,
+               int64_t r0, int64_t c0, int64_t rr, int64_t cc, bool lines_are_rows, int* out_slot,
+               int* staging_turn) {
+  int idx = cache.find(key);
+  if (idx >= 0) {
+    cache.slots[idx].stamp = ++cache.clock;
+    ctx->stats.tiles_reused++;
+    *out_slot = idx;
+    return TMM_SUCCESS;
+  }
+  idx = cache.victim();
+  tmm::Slot& s = cache.slots[idx];
+  if (s.key >= 0) cache.index.erase(s.key);
+  const char* src = h.ptr + ((size_t)r0 + (size_t)c0 * (size_t)h.ld) * P.es;
+  if (!P.ozaki) {
+    if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, s.last_use, 0));
+    TMM_CUDA(ctx, cudaMemcpy2DAsync(s.ptr, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
+                                    (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
+    TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));
+  } else {
+    // raw tile -> staging buffer (ring of 3) on the copy stream; split -> slot on the prep stream
+    int turn = (*staging_turn)++ % 3;
+    char* stage = (char*)ctx->staging.ptr + (size_t)turn * ((P.staging_bytes + 255) / 256 * 256);
+    TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->staging_free[turn], 0));
+    TMM_CUDA(ctx, cudaMemcpy2DAsync(stage, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
+                                    (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
+    TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));  // reused below as "staged"
+    TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->prep, s.ready, 0));
+    if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->prep, s.last_use, 0));
+    // lines along k: for A (lines = rows of op(A)); for B (lines = columns of op(B))
+    int64_t lines = lines_are_rows ? rr : cc;   // stored orientation resolved by caller
+    int64_t kk = lines_are_rows ? cc : rr;
+    Op t = lines_are_rows ? tmm::OP_N : tmm::OP_T;
+    tmm::OzakiSplit v = tmm::ozaki_split_view(s.ptr, lines, kk, P.slices);
+    cudaError_t e = tmm::ozaki_split((const double*)stage, rr, t, lines, kk, v, ctx->prep);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki split launch");
+    ctx->stats.kernels++;
+    TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->prep));
+    TMM_CUDA(ctx, cudaEventRecord(ctx->staging_free[turn], ctx->prep));
+  }
+  ctx->stats.h2d_bytes += (uint64_t)rr * (uint64_t)cc * P.es;
+  ctx->stats.tiles_loaded++;
+  s.key = key;
+  s.stamp = ++cache.clock;
+  cache.index[key] = idx;
+  *out_slot = idx;
+  return TMM_SUCCESS;
+}
+
+int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_t lda, const void* b,
+             int64_t ldb, const void* beta, void* c, int64_t ldc, bool copy_back) {
+  const bool beta_nz = !is_zero(ctx->dtype, beta);
+  const int ns = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->n_streams, P.ntm * P.ntn));  // tiled_mm.cpp:284
+
+  // ---- memory
+  size_t n_a = 0, n_b = 0;
+  int st = plan_memory(ctx, P, copy_back, &n_a, &n_b);
+  if (st) return st;
+  if (P.ntk > 0) {
+    st = setup_cache(ctx, ctx->cache_a, ctx->pool_a, n_a, P.a_slot_bytes);
+    if (st) return st;
+    st = setup_cache(ctx, ctx->cache_b, ctx->pool_b, n_b, P.b_slot_bytes);
+    if (st) return st;
+  }
+  if (P.ozaki) {
+    size_t sb = (P.staging_bytes + 255) / 256 * 256;
+    TMM_CUDA(ctx, ctx->staging.reserve(3 * sb));
+    while (ctx->staging_free.size() < 3) {
+      cudaEvent_t e;
+      TMM_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ctx->staging_free.push_back(e);
+    }
+    // staging buffers start free
+    for (auto e : ctx->staging_free) TMM_CUDA(ctx, cudaEventRecord(e, ctx->prep));
+  }
+  if (copy_back) {
+    size_t cb = (P.c_slot_bytes + 255) / 256 * 256;
+    TMM_CUDA(ctx, ctx->pool_c.reserve(2 * (size_t)ns * cb));
+    while ((int)ctx->cslots.size() < 2 * ns) ctx->cslots.push_back(tmm::CSlot());
+    for (int i = 0; i < 2 * ns; ++i) {
+      if (!ctx->cslots[i].done) TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->cslots[i].done, cudaEventDisableTiming));
+      ctx->cslots[i].ptr = (char*)ctx->pool_c.ptr + (size_t)i * cb;
+      ctx->cslots[i].used = false;
+    }
+  } else {
+    TMM_CUDA(ctx, ctx->full_c.reserve((size_t)P.m * (size_t)P.n * P.es));
+    ctx->full_c_elems = (size_t)P.m * (size_t)P.n;
+  }
+
+  // everything queued on this context's streams starts after earlier work on them
+  HostMat A{(const char*)a, lda}, B{(const char*)b, ldb};
+  const char* Ch = (const char*)c;
+  int staging_turn = 0;
+  char one[16] = {0};  // the scalar 1 of the context's dtype (beta' of later k-tiles)
+  switch (ctx->dtype) {
+    case TMM_FLOAT: *(float*)one = 1.f; break;
+    case TMM_DOUBLE: *(double*)one = 1.0; break;
+    case TMM_COMPLEX_FLOAT: ((float*)one)[0] = 1.f; break;
+    default: ((double*)one)[0] = 1.0;
+  }
+
+  int64_t t = 0;
+  for (int64_t i = 0; i < P.ntm; ++i) {
+    const int64_t mi = extent(P.m, P.tm, i), r0 = i * P.tm;
+    for (int64_t jj = 0; jj < P.ntn; ++jj, ++t) {
+      const int64_t j = (i & 1) ? (P.ntn - 1 - jj) : jj;  // snake order: reuse the last B tiles
+      const int64_t nj = extent(P.n, P.tn, j), c0 = j * P.tn;
+      const int sidx = (int)(t % ns);
+      cudaStream_t s = ctx->streams[sidx];
+      char* ct;
+      int64_t ldct;
+      tmm::CSlot* cs = nullptr;
+      if (copy_back) {
+        cs = &ctx->cslots[(size_t)sidx * 2 + (size_t)((t / ns) & 1)];
+        if (cs->used) TMM_CUDA(ctx, cudaStreamWaitEvent(s, cs->done, 0));
+        ct = cs->ptr;
+        ldct = mi;
+      } else {
+        ct = (char*)ctx->full_c.ptr + ((size_t)r0 + (size_t)c0 * (size_t)P.m) * P.es;
+        ldct = P.m;
+      }
+      if (beta_nz) {  // the C tile is read only when beta != 0 (tiled_mm.cpp:325-330, 425-431)
+        TMM_CUDA(ctx, cudaMemcpy2DAsync(ct, (size_t)ldct * P.es, Ch + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es,
+                                        (size_t)ldc * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyHostToDevice, s));
+        ctx->stats.h2d_bytes += (uint64_t)mi * (uint64_t)nj * P.es;
+      }
+      if (P.ntk == 0) {
+        st = launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, 0, alpha, nullptr, 1, nullptr, 1, beta, ct, ldct, s);
+        if (st) return st;
+      }
+      for (int64_t kt = 0; kt < P.ntk; ++kt) {
+        const int64_t kk = extent(P.k, P.tk, kt), k0 = kt * P.tk;
+        int sa = -1, sb = -1;
+        // A tile (i, kt): stored block rows/cols depend on op(A)
+        if (P.opa == tmm::OP_N)
+          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, r0, k0, mi, kk, true, &sa, &staging_turn);
+        else
+          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, k0, r0, kk, mi, false, &sa, &staging_turn);
+        if (st) return st;
+        if (P.opb == tmm::OP_N)
+          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, k0, c0, kk, nj, false, &sb, &staging_turn);
+        else
+          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, c0, k0, nj, kk, true, &sb, &staging_turn);
+        if (st) return st;
+        tmm::Slot& SA = ctx->cache_a.slots[sa];
+        tmm::Slot& SB = ctx->cache_b.slots[sb];
+        TMM_CUDA(ctx, cudaStreamWaitEvent(s, SA.ready, 0));
+        TMM_CUDA(ctx, cudaStreamWaitEvent(s, SB.ready, 0));
+        const void* bk = kt == 0 ? beta : (const void*)one;
+        if (!P.ozaki) {
+          const int64_t lda_t = P.opa == tmm::OP_N ? mi : kk;
+          const int64_t ldb_t = P.opb == tmm::OP_N ? kk : nj;
+          st = launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s);
+          if (st) return st;
+        } else {
+          tmm::OzakiSplit va = tmm::ozaki_split_view(SA.ptr, mi, kk, P.slices);
+          tmm::OzakiSplit vb = tmm::ozaki_split_view(SB.ptr, nj, kk, P.slices);
+          cudaError_t e = tmm::ozaki_gemm(va, vb, mi, nj, *(const double*)alpha, *(const double*)beta, kt == 0,
+                                          (double*)ct, ldct, s);
+          if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki gemm launch");
+          ctx->stats.kernels++;
+        }
+        TMM_CUDA(ctx, cudaEventRecord(SA.last_use, s));
+        TMM_CUDA(ctx, cudaEventRecord(SB.last_use, s));
+        SA.used = SB.used = true;
+      }
+      if (copy_back) {  // result stream copies the finished tile back (tiled_mm.cpp:350-358)
+        TMM_CUDA(ctx, cudaEventRecord(cs->done, s));
+        TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h, cs->done, 0));
+        TMM_CUDA(ctx, cudaMemcpy2DAsync((char*)c + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es, (size_t)ldc * P.es,
+                                        ct, (size_t)ldct * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDeviceToHost,
+                                        ctx->d2h));
+        TMM_CUDA(ctx, cudaEventRecord(cs->done, ctx->d2h));
+        cs->used = true;
+        ctx->stats.d2h_bytes += (uint64_t)mi * (uint64_t)nj * P.es;
+      }
+    }
+  }
+  return TMM_SUCCESS;
+}
+
+int sync_all(tmm_context* ctx) {
+  cudaError_t first = cudaSuccess;
+  for (auto s : ctx->streams) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (first == cudaSuccess) first = e;
+  }
+  for (cudaStream_t s : {ctx->h2d, ctx->prep, ctx->d2h}) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (first == cudaSuccess) first = e;
+  }
+  if (first != cudaSuccess) return cuda_fail(ctx, first, "stream synchronize");
+  return TMM_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
+                        const void* alpha, const void* a, int64_t ld_a, const void* b, int64_t ld_b,
+                        const void* beta, void* c, int64_t ld_c, int pin_host_buffers, int copy_c_back) {
+  if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: null context");
+  auto t0 = std::chrono::steady_clock::now();
+  ctx->stats = tmm_stats{};
+  Plan P{};
+  if (!parse_op(trans_a, ctx->dtype, &P.opa) || !parse_op(trans_b, ctx->dtype, &P.opb))
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: trans must be one of N, T, C");
+  if (m < 0 || n < 0 || k < 0) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: negative size");
+  if (!alpha || !beta) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: null alpha or beta");
+  const int64_t a_rows = P.opa == tmm::OP_N ? m : k, a_cols = P.opa == tmm::OP_N ? k : m;
+  const int64_t b_rows = P.opb == tmm::OP_N ? k : n, b_cols = P.opb == tmm::OP_N ? n : k;
+  // leading-dimension checks of src/Tiled-MM/tiled_mm.cpp:516-527, enforced here
+  if (ld_a < std::max<int64_t>(1, a_rows)) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: ld_a < rows of A");
+  if (ld_b < std::max<int64_t>(1, b_rows)) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: ld_b < rows of B");
+  if (ld_c < std::max<int64_t>(1, m)) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: ld_c < rows of C");
+  if (m == 0 || n == 0) return TMM_SUCCESS;
+  const bool beta_nz = !is_zero(ctx->dtype, beta);
+  if ((k > 0 && (!a || !b)) || ((copy_c_back || beta_nz) && !c))
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: null matrix pointer");
+  const bool ozaki = ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE;
+  DeviceGuard dg(ctx->device);
+
+  // ---- tile sizes (src/Tiled-MM/tiled_mm.cpp:557-560)
+  int tm, tn, tk;
+  if (ctx->tile_policy == TMM_TILE_POLICY_REFERENCE) {
+    tm = optimal_tile_size(m, ctx->cur_tile_m, ctx->max_tile_m);
+    tn = optimal_tile_size(n, ctx->cur_tile_n, ctx->max_tile_n);
+    tk = optimal_tile_size(std::max<int64_t>(k, 1), ctx->cur_tile_k, ctx->max_tile_k);
+  } else {
+    tm = (int)std::min<int64_t>(m, ctx->max_tile_m);
+    tn = (int)std::min<int64_t>(n, ctx->max_tile_n);
+    tk = (int)std::min<int64_t>(std::max<int64_t>(k, 1), ctx->max_tile_k);
+  }
+  ctx->cur_tile_m = tm;
+  ctx->cur_tile_n = tn;
+  ctx->cur_tile_k = tk;
+  P.m = m; P.n = n; P.k = k; P.tm = tm; P.tn = tn; P.tk = tk;
+  P.ntm = ntiles(m, tm); P.ntn = ntiles(n, tn); P.ntk = ntiles(k, tk);
+  P.es = elem_size(ctx->dtype);
+  P.ozaki = ozaki;
+  P.slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+  if (ozaki) {
+    P.a_slot_bytes = tmm::ozaki_split_bytes(tm, tk, P.slices);
+    P.b_slot_bytes = tmm::ozaki_split_bytes(tn, tk, P.slices);
+    P.staging_bytes = (size_t)std::max(tm, tn) * (size_t)tk * 8;
+  } else {
+    P.a_slot_bytes = (size_t)tm * (size_t)tk * P.es;
+    P.b_slot_bytes = (size_t)tk * (size_t)tn * P.es;
+    P.staging_bytes = 0;
+  }
+  P.c_slot_bytes = (size_t)tm * (size_t)tn * P.es;
+
+  // ---- pin (src/Tiled-MM/tiled_mm.cpp:529-554)
+  Pin pa, pb, pc;
+  int st = TMM_SUCCESS;
+  if (pin_host_buffers) {
+    if (k > 0) {
+      st = pin_range(ctx, a, ((size_t)ld_a * (size_t)(a_cols - 1) + (size_t)a_rows) * P.es, &pa);
+      if (!st) st = pin_range(ctx, b, ((size_t)ld_b * (size_t)(b_cols - 1) + (size_t)b_rows) * P.es, &pb);
+    }
+    if (!st && (copy_c_back || beta_nz))
+      st = pin_range(ctx, c, ((size_t)ld_c * (size_t)(n - 1) + (size_t)m) * P.es, &pc);
+  }
+  ctx->stats.tile_m = tm;
+  ctx->stats.tile_n = tn;
+  ctx->stats.tile_k = tk;
+  ctx->stats.n_streams = (int)std::min<int64_t>(ctx->n_streams, P.ntm * P.ntn);
+  ctx->stats.path = ozaki ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
+  ctx->stats.ozaki_slices = ozaki ? P.slices : 0;
+  if (!st) st = run_gemm(ctx, P, alpha, a, ld_a, b, ld_b, beta, c, ld_c, copy_c_back != 0);
+  int st2 = sync_all(ctx);  // returns with C final (the reference syncs the device: tiled_mm.cpp:602-604)
+  if (!st) st = st2;
+  unpin(pa);
+  unpin(pb);
+  unpin(pc);
+  ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
+                               const void* alpha, const void* a, int64_t ld_a, const void* b, int64_t ld_b,
+                               const void* beta, void* c, int64_t ld_c, void* stream) {
+  if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: null context");
+  ctx->stats = tmm_stats{};
+  Op opa, opb;
+  if (!parse_op(trans_a, ctx->dtype, &opa) || !parse_op(trans_b, ctx->dtype, &opb))
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: trans must be one of N, T, C");
+  if (m < 0 || n < 0 || k < 0 || !alpha || !beta)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: bad size or scalar");
+  const int64_t a_rows = opa == tmm::OP_N ? m : k, b_rows = opb == tmm::OP_N ? k : n;
+  if (ld_a < std::max<int64_t>(1, a_rows) || ld_b < std::max<int64_t>(1, b_rows) || ld_c < std::max<int64_t>(1, m))
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: leading dimension too small");
+  if (m == 0 || n == 0) return TMM_SUCCESS;
+  if ((k > 0 && (!a || !b)) || !c) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: null matrix pointer");
+  DeviceGuard dg(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->streams[0];
+  if (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE && k > 0) {
+    // split op(A) and op(B) in k-tiles of at most tile_k (per-k-tile scaling) into scratch, then multiply
+    const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+    const int64_t tk = std::min<int64_t>(k, ctx->max_tile_k);
+    const size_t sa = tmm::ozaki_split_bytes(m, tk, slices), sb = tmm::ozaki_split_bytes(n, tk, slices);
+    const size_t sa_al = (sa + 255) / 256 * 256;
+    TMM_CUDA(ctx, ctx->scratch.reserve(sa_al + sb));
+    for (int64_t k0 = 0, kt = 0; k0 < k; k0 += tk, ++kt) {
+      const int64_t kk = std::min(tk, k - k0);
+      tmm::OzakiSplit va = tmm::ozaki_split_view(ctx->scratch.ptr, m, kk, slices);
+      tmm::OzakiSplit vb = tmm::ozaki_split_view((char*)ctx->scratch.ptr + sa_al, n, kk, slices);
+      const double* ab = opa == tmm::OP_N ? (const double*)a + k0 * ld_a : (const double*)a + k0;
+      const double* bb = opb == tmm::OP_N ? (const double*)b + k0 : (const double*)b + k0 * ld_b;
+      cudaError_t e = tmm::ozaki_split(ab, ld_a, opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, m, kk, va, s);
+      if (e == cudaSuccess) e = tmm::ozaki_split(bb, ld_b, opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, n, kk, vb, s);
+      if (e == cudaSuccess)
+        e = tmm::ozaki_gemm(va, vb, m, n, *(const double*)alpha, *(const double*)beta, kt == 0, (double*)c, ld_c, s);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki device gemm launch");
+      ctx->stats.kernels += 3;
+    }
+    return TMM_SUCCESS;
+  }
+  return launch_tile_gemm(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s);
+}
+
+// ------------------------------------------------------------------ utilities
+extern "C" int tmm_malloc_pinned(size_t bytes, void** p) {
+  if (!p) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_malloc_pinned: null output");
+  cudaError_t e = cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostAlloc");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_free_pinned(void* p) {
+  if (!p) return TMM_SUCCESS;
+  cudaError_t e = cudaFreeHost(p);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaFreeHost");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_copy_to_device(const void* h, void* d, size_t bytes) {
+  cudaError_t e = cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemcpy H2D");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_copy_to_host(const void* d, void* h, size_t bytes) {
+  cudaError_t e = cudaMemcpy(h, d, bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemcpy D2H");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_memcpy_async(void* dst, const void* src, size_t bytes, void* stream) {
+  if ((!dst || !src) && bytes) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_memcpy_async: null pointer");
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemcpyAsync");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_malloc_device(size_t bytes, void** p) {
+  if (!p) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_malloc_device: null output");
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  return TMM_SUCCESS;
+}
+extern "C" int tmm_free_device(void* p) {
+  if (!p) return TMM_SUCCESS;
+  cudaError_t e = cudaFree(p);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaFree");
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_fill_host_f64(double* x, int64_t rows, int64_t cols, int64_t ld, int kind, double param,
+                                 uint64_t seed, uint64_t id, int n_threads) {
+  if (!x || rows < 0 || cols < 0 || ld < rows) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_fill_host_f64: bad arguments");
+  if (n_threads < 1) n_threads = 1;
+  auto work = [&](int t) {
+    int64_t c0 = cols * t / n_threads, c1 = cols * (t + 1) / n_threads;
+    for (int64_t j = c0; j < c1; ++j)
+      for (int64_t i = 0; i < rows; ++i) x[i + j * ld] = tmm_gen_value(kind, param, seed, id, i, j, rows);
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < n_threads; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& h : th) h.join();
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_fill_device_f64(double* x, int64_t rows, int64_t cols, int64_t ld, int kind, double param,
+                                   uint64_t seed, uint64_t id, void* stream) {
+  if (!x || rows < 0 || cols < 0 || ld < rows) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_fill_device_f64: bad arguments");
+  cudaError_t e = tmm::launch_fill_f64(x, rows, cols, ld, kind, param, seed, id, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "fill kernel launch");
+  return TMM_SUCCESS;
+}
+
+// Compensated dot products (TwoSum / TwoProduct, Ogita-Rump-Oishi 2005) over
+// sampled entries: the FP64-oracle error metric reported with every result.
+extern "C" int tmm_error_metric_f64(char trans_a, char trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                                    const double* a, int64_t lda, const double* b, int64_t ldb, double beta,
+                                    const double* c0, int64_t ldc0, const double* c, int64_t ldc, int64_t ns,
+                                    uint64_t seed, int n_threads, double* metric) {
+  if (!metric || !c || m <= 0 || n <= 0 || k < 0 || ns <= 0 || (k > 0 && (!a || !b)) || (beta != 0.0 && !c0))
+    return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_error_metric_f64: bad arguments");
+  const bool ta = upper(trans_a) != 'N', tb = upper(trans_b) != 'N';
+  if (n_threads < 1) n_threads = 1;
+  std::vector<double> worst(n_threads, 0.0);
+  auto work = [&](int t) {
+    for (int64_t s = t; s < ns; s += n_threads) {
+      uint64_t h = tmm_splitmix64(seed ^ (uint64_t)s * 0x9E3779B97F4A7C15ull);
+      int64_t i = (int64_t)(h % (uint64_t)m), j = (int64_t)((h >> 32) % (uint64_t)n);
+      if (s == 0) { i = 0; j = 0; }
+      if (s == 1) { i = m - 1; j = n - 1; }
+      double sum = 0, err = 0, mag = 0;
+      for (int64_t l = 0; l < k; ++l) {
+        double x = ta ? a[l + i * lda] : a[i + l * lda];
+        double y = tb ? b[j + l * ldb] : b[l + j * ldb];
+        double p = x * y, pe = std::fma(x, y, -p);
+        double s2 = sum + p, z = s2 - sum, se = (sum - (s2 - z)) + (p - z);
+        sum = s2;
+        err += pe + se;
+        mag += std::fabs(x) * std::fabs(y);
+      }
+      double hi = alpha * sum, lo = std::fma(alpha, sum, -hi) + alpha * err;
+      mag *= std::fabs(alpha);
+      if (beta != 0.0) {
+        double cv = c0[i + j * ldc0];
+        double p = beta * cv, pe = std::fma(beta, cv, -p);
+        double s2 = hi + p, z = s2 - hi, se = (hi - (s2 - z)) + (p - z);
+        hi = s2;
+        lo += se + pe;
+        mag += std::fabs(beta) * std::fabs(cv);
+      }
+      double ref = hi + lo, got = c[i + j * ldc];
+      double d = std::fabs(got - ref);
+      double r;
+      if (d != d) r = INFINITY;
+      else if (mag == 0) r = d == 0 ? 0.0 : INFINITY;
+      else r = d / ((double)std::max<int64_t>(k, 1) * 1.1102230246251565e-16 * mag);
+      if (r > worst[t] || r != r) worst[t] = r;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < n_threads; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& h : th) h.join();
+  double w = 0;
+  for (double v : worst) w = std::max(w, v);
+  *metric = w;
+  return TMM_SUCCESS;
+}

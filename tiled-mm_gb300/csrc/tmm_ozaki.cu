@@ -1,0 +1,357 @@
+// Ozaki split-precision FP64 GEMM: the emulated-DGEMM path.
+//
+// Algorithm (published; no counterpart in the reference, which calls
+// cublasDgemm per tile, src/Tiled-MM/tiled_mm.cpp:200-217):
+//   Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix
+//   multiplication by using fast routines of matrix multiplication and its
+//   applications", Numer. Algorithms 59 (2012) -- error-free splitting;
+//   Mukunoki, Ozaki, Ogita, Imamura, "DGEMM using tensor cores, and its
+//   accurate and reproducible versions", ISC 2020; Ootomo, Ozaki, Yokota,
+//   "DGEMM on integer matrix multiplication unit", IJHPCA 2024 -- integer
+//   slices on tensor cores.
+//
+//  1. scale (FP64): line r of op(A) (rows) / op(B) (columns) over the tile's k
+//     range gets e_r = frexp exponent of its largest magnitude.
+//  2. split (FP64, exact): t = x * 2^-e * 16; for p < s: d_p = rint(t),
+//     t = (t - d_p) * 32.  |d_p| <= 16, so a digit is exact in int8 and in
+//     e4m3.  x = 2^e * sum_p d_p 2^(-4 - 5p) + O(2^(e - 5s - 5)).
+//  3. multiply (tensor cores, exact): for each diagonal g = s-1 .. 0 of the
+//     slice-pair triangle, sum over pairs (p, g-p) of the integer tile
+//     products; partial sums are exact integers (|d_a d_b| <= 256).
+//  4. recombine (FP64): acc += 2^(-5 g) * S after each exactness pass;
+//     t = acc * 2^(e_i + f_j - 8); C = fma(alpha, t, beta' * C).
+// The oracle (oracle/tmm_ozaki_oracle.c) performs the same FP64 operations in
+// the same order, so results agree bit for bit.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "tmm_ozaki.h"
+
+namespace tmm {
+
+// ------------------------------------------------------------------ configuration
+int ozaki_engine() {
+  static int engine = [] {
+    const char* e = getenv("TMM_OZAKI_ENGINE");
+    if (e && strcmp(e, "imma") == 0) return (int)OZ_ENGINE_IMMA;
+    if (e && strcmp(e, "tcgen05") == 0) return (int)OZ_ENGINE_TCGEN05;
+    return (int)OZ_ENGINE_IMMA;
+  }();
+  return engine;
+}
+
+int ozaki_encoding() { return ozaki_engine() == OZ_ENGINE_TCGEN05 ? OZ_ENC_E4M3 : OZ_ENC_INT8; }
+
+size_t ozaki_split_bytes(int64_t rows, int64_t kk, int slices) {
+  int64_t rp = oz_round_up(rows > 0 ? rows : 1, OZ_ROW_ALIGN);
+  int64_t kp = oz_round_up(kk > 0 ? kk : 1, OZ_K_ALIGN);
+  size_t digits = (size_t)slices * (size_t)rp * (size_t)kp;
+  digits = (digits + 1023) / 1024 * 1024;
+  return digits + (size_t)rp * sizeof(int32_t);
+}
+
+OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices) {
+  OzakiSplit v;
+  v.rows = rows;
+  v.kk = kk;
+  v.rows_pad = oz_round_up(rows > 0 ? rows : 1, OZ_ROW_ALIGN);
+  v.k_pad = oz_round_up(kk > 0 ? kk : 1, OZ_K_ALIGN);
+  v.slices = slices;
+  v.enc = ozaki_encoding();
+  size_t digits = (size_t)slices * (size_t)v.rows_pad * (size_t)v.k_pad;
+  digits = (digits + 1023) / 1024 * 1024;
+  v.digits = (uint8_t*)base;
+  v.exps = (int32_t*)((char*)base + digits);
+  return v;
+}
+
+namespace {
+
+// ------------------------------------------------------------------ split
+__device__ __forceinline__ uint32_t digit_byte(int d, int enc) {
+  if (enc == OZ_ENC_INT8) return (uint32_t)(uint8_t)(int8_t)d;
+  uint32_t a = (uint32_t)(d < 0 ? -d : d);
+  if (a == 0) return 0;
+  int e = 31 - __clz(a);                  // floor(log2 a), a <= 16
+  uint32_t mant = ((a << 3) >> e) & 7u;   // 3 fraction bits (exact for a <= 16)
+  return (d < 0 ? 0x80u : 0u) | ((uint32_t)(e + 7) << 3) | mant;
+}
+
+constexpr int SP_LINES = 32, SP_L = 64, SP_THREADS = 256;
+
+template <int TRANS>
+__global__ void __launch_bounds__(SP_THREADS)
+oz_split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, uint8_t* __restrict__ digits,
+                int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc) {
+  __shared__ double tile[SP_LINES][SP_L + 1];
+  __shared__ double red[8][SP_LINES];
+  __shared__ int sexp[SP_LINES];
+  const int tid = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * SP_LINES;
+
+  // ---- phase 1: largest magnitude of each line
+  if (TRANS == 0) {
+    const int r = tid & 31, lg = tid >> 5;
+    double mx = 0.0;
+    if (r0 + r < rows)
+      for (int64_t l = lg; l < kk; l += 8) mx = fmax(mx, fabs(X[(r0 + r) + l * ld]));
+    red[lg][r] = mx;
+  } else {
+    const int lane = tid & 31, w = tid >> 5;
+    for (int rr = w; rr < SP_LINES; rr += 8) {
+      double mx = 0.0;
+      if (r0 + rr < rows)
+        for (int64_t l = lane; l < kk; l += 32) mx = fmax(mx, fabs(X[l + (r0 + rr) * ld]));
+      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0) red[0][rr] = mx;
+    }
+  }
+  __syncthreads();
+  if (tid < SP_LINES) {
+    double mx = red[0][tid];
+    if (TRANS == 0)
+      for (int q = 1; q < 8; ++q) mx = fmax(mx, red[q][tid]);
+    int e = 0;
+    if (mx != 0.0) frexp(mx, &e);
+    sexp[tid] = e;
+    exps[r0 + tid] = e;
+  }
+  __syncthreads();
+
+  // ---- phase 2: digits, 32 lines x 64 k per step, 8 consecutive k per thread
+  const size_t plane = (size_t)rows_pad * (size_t)k_pad;
+  for (int64_t l0 = 0; l0 < k_pad; l0 += SP_L) {
+    if (TRANS == 0) {
+      const int r = tid & 31, cg = tid >> 5;
+      for (int c = cg; c < SP_L; c += 8) {
+        int64_t l = l0 + c;
+        tile[r][c] = (r0 + r < rows && l < kk) ? X[(r0 + r) + l * ld] : 0.0;
+      }
+    } else {
+      const int c = tid & 63, rq = tid >> 6;
+      for (int r = rq; r < SP_LINES; r += 4) {
+        int64_t l = l0 + c;
+        tile[r][c] = (r0 + r < rows && l < kk) ? X[l + (r0 + r) * ld] : 0.0;
+      }
+    }
+    __syncthreads();
+    {
+      const int r = tid >> 3, c8 = (tid & 7) * 8;
+      const int e = sexp[r];
+      double t[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) t[q] = scalbn(tile[r][c8 + q], -e) * 16.0;
+      uint8_t* dst = digits + (size_t)(r0 + r) * (size_t)k_pad + (size_t)(l0 + c8);
+      for (int p = 0; p < s; ++p) {
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          double d = rint(t[q]);
+          t[q] = (t[q] - d) * 32.0;
+          uint32_t b = digit_byte((int)d, enc);
+          if (q < 4) lo |= b << (8 * q);
+          else hi |= b << (8 * (q - 4));
+        }
+        *reinterpret_cast<uint2*>(dst + (size_t)p * plane) = make_uint2(lo, hi);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ IMMA engine
+// Exact int8 x int8 -> int32 tile products with mma.sync m16n8k32 (the
+// legacy integer tensor path).  CTA tile 128 x 128, 8 warps of 64 x 32,
+// k-blocks of 64 bytes in a 2-stage cp.async pipeline; the FP64 accumulators
+// live in shared memory (each thread owns its positions) and are updated
+// once per exactness pass.
+constexpr int IM_BM = 128, IM_BN = 128, IM_KB = 64, IM_THREADS = 256;
+constexpr int IM_STRIDE = IM_KB + 16;  // bytes; conflict-free fragment loads
+constexpr int IM_STAGE = (IM_BM + IM_BN) * IM_STRIDE;
+constexpr size_t IM_SMEM = 2 * IM_STAGE + (size_t)IM_BM * IM_BN * sizeof(double);
+constexpr int64_t IM_PASS_BLOCKS = 65536;  // 65536 * 64 terms * 256 < 2^31
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void imma_16x8x32(int (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct IterState {
+  int g, p, kb;
+};
+
+__global__ void __launch_bounds__(IM_THREADS, 1)
+oz_gemm_imma(const uint8_t* __restrict__ Ad, const int32_t* __restrict__ ea, int64_t a_rows_pad,
+             const uint8_t* __restrict__ Bd, const int32_t* __restrict__ eb, int64_t b_rows_pad, int64_t k_pad,
+             int s, int64_t m, int64_t n, double alpha, double beta, int first, double* __restrict__ C,
+             int64_t ldc, int64_t pass_blocks) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  double* facc = reinterpret_cast<double*>(smem + 2 * IM_STAGE);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g8 = lane >> 2, t4 = lane & 3;
+  const int wm = (warp & 1) * 64, wn = (warp >> 1) * 32;
+  const int64_t i0 = (int64_t)blockIdx.x * IM_BM, j0 = (int64_t)blockIdx.y * IM_BN;
+  const int64_t nkb = k_pad / IM_KB;
+  const size_t plane_a = (size_t)a_rows_pad * (size_t)k_pad, plane_b = (size_t)b_rows_pad * (size_t)k_pad;
+
+  // fragment-owned FP64 accumulator positions: (mi, ni, c) -> row, col in the CTA tile
+  for (int q = tid; q < IM_BM * IM_BN; q += IM_THREADS) facc[q] = 0.0;
+
+  int acc[4][4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0;
+
+  auto load_stage = [&](int stage, const IterState& it) {
+    uint8_t* sa = smem + stage * IM_STAGE;
+    uint8_t* sb = sa + IM_BM * IM_STRIDE;
+    const uint8_t* ga = Ad + (size_t)it.p * plane_a + (size_t)i0 * (size_t)k_pad + (size_t)it.kb * IM_KB;
+    const uint8_t* gb = Bd + (size_t)(it.g - it.p) * plane_b + (size_t)j0 * (size_t)k_pad + (size_t)it.kb * IM_KB;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      int chunk = tid + q * IM_THREADS;  // 512 chunks of 16 bytes per operand
+      int row = chunk >> 2, col = (chunk & 3) * 16;
+      cp_async16(sa + row * IM_STRIDE + col, ga + (size_t)row * (size_t)k_pad + col);
+      cp_async16(sb + row * IM_STRIDE + col, gb + (size_t)row * (size_t)k_pad + col);
+    }
+  };
+  auto advance = [&](IterState& it) {
+    if (++it.kb == nkb) {
+      it.kb = 0;
+      if (++it.p > it.g) {
+        it.p = 0;
+        --it.g;
+      }
+    }
+  };
+
+  IterState cur{s - 1, 0, 0};
+  IterState nxt = cur;
+  advance(nxt);
+  load_stage(0, cur);
+  cp_async_commit();
+  int64_t used = 0;
+  int stage = 0;
+  while (cur.g >= 0) {
+    if (nxt.g >= 0) load_stage(stage ^ 1, nxt);
+    cp_async_commit();
+    cp_async_wait1();
+    __syncthreads();
+    const uint8_t* sa = smem + stage * IM_STAGE;
+    const uint8_t* sb = sa + IM_BM * IM_STRIDE;
+#pragma unroll
+    for (int ks = 0; ks < IM_KB; ks += 32) {
+      uint32_t af[4][4], bf[4][2];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const uint8_t* base = sa + (wm + a * 16 + g8) * IM_STRIDE + ks + 4 * t4;
+        af[a][0] = *reinterpret_cast<const uint32_t*>(base);
+        af[a][1] = *reinterpret_cast<const uint32_t*>(base + 8 * IM_STRIDE);
+        af[a][2] = *reinterpret_cast<const uint32_t*>(base + 16);
+        af[a][3] = *reinterpret_cast<const uint32_t*>(base + 8 * IM_STRIDE + 16);
+      }
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const uint8_t* base = sb + (wn + b * 8 + g8) * IM_STRIDE + ks + 4 * t4;
+        bf[b][0] = *reinterpret_cast<const uint32_t*>(base);
+        bf[b][1] = *reinterpret_cast<const uint32_t*>(base + 16);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) imma_16x8x32(acc[a][b], af[a], bf[b]);
+    }
+    __syncthreads();
+    // pass boundary: at the block cap or at the end of the diagonal
+    ++used;
+    const bool group_end = (cur.kb == nkb - 1) && (cur.p == cur.g);
+    if (used == pass_blocks || group_end) {
+      const double wg = scalbn(1.0, -OZ_DIGIT_BITS * cur.g);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            int row = wm + a * 16 + g8 + ((c >> 1) << 3), col = wn + b * 8 + 2 * t4 + (c & 1);
+            double* f = facc + row * IM_BN + col;
+            *f = *f + wg * (double)acc[a][b][c];
+            acc[a][b][c] = 0;
+          }
+      used = 0;
+    }
+    cur = nxt;
+    advance(nxt);
+    stage ^= 1;
+  }
+  cp_async_wait0();
+  // fused epilogue
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        int row = wm + a * 16 + g8 + ((c >> 1) << 3), col = wn + b * 8 + 2 * t4 + (c & 1);
+        int64_t gi = i0 + row, gj = j0 + col;
+        if (gi < m && gj < n) {
+          double t = scalbn(facc[row * IM_BN + col], ea[gi] + eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
+          double* cp = C + gi + gj * ldc;
+          if (!first) *cp = fma(alpha, t, *cp);
+          else if (beta != 0.0) *cp = fma(alpha, t, beta * *cp);
+          else *cp = alpha * t;
+        }
+      }
+}
+
+}  // namespace
+
+int64_t ozaki_pass_blocks() { return IM_PASS_BLOCKS; }
+int64_t ozaki_k_block() { return IM_KB; }
+
+cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int64_t kk, const OzakiSplit& out,
+                        cudaStream_t s) {
+  if (out.slices < 1 || out.slices > OZ_MAX_SLICES) return cudaErrorInvalidValue;
+  unsigned blocks = (unsigned)(out.rows_pad / SP_LINES);
+  if (trans == OP_N)
+    oz_split_kernel<0><<<blocks, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
+                                                     out.slices, out.enc);
+  else
+    oz_split_kernel<1><<<blocks, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
+                                                     out.slices, out.enc);
+  return cudaGetLastError();
+}
+
+cudaError_t ozaki_gemm(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
+                       bool first_k_tile, double* C, int64_t ldc, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  if (A.k_pad != B.k_pad || A.slices != B.slices || A.rows_pad < m || B.rows_pad < n) return cudaErrorInvalidValue;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(oz_gemm_imma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)IM_SMEM);
+  });
+  if (attr_err != cudaSuccess) return attr_err;
+  dim3 grid((unsigned)((m + IM_BM - 1) / IM_BM), (unsigned)((n + IM_BN - 1) / IM_BN));
+  oz_gemm_imma<<<grid, IM_THREADS, IM_SMEM, s>>>(A.digits, A.exps, A.rows_pad, B.digits, B.exps, B.rows_pad, A.k_pad,
+                                                 A.slices, m, n, alpha, beta, first_k_tile ? 1 : 0, C, ldc,
+                                                 IM_PASS_BLOCKS);
+  return cudaGetLastError();
+}
+
+}  // namespace tmm
