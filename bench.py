@@ -42,6 +42,9 @@ WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                        path="ozaki", tiles=(32768, 32768, 32768), streams=2,
                        desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20]"),
+    "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
+                      path="ozaki", tiles=(8192, 8192, 8192), streams=2,
+                      desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
     "native4096": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=1.0, kind=0, param=0.0,
                        path="native", tiles=(2048, 2048, 2048), streams=2,
                        desc="FP64 GEMM m=n=k=4096 NN, uniform[-1,1), alpha=beta=1, tiles 2048, 2 streams"),

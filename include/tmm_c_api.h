@@ -101,7 +101,7 @@ int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n,
              const void* beta, void* c, int64_t ld_c, int pin_host_buffers, int copy_c_back);
 
 /* Same product on operands already in device memory (no host copies), on the
- * given CUDA stream (a cudaStream_t, or NULL for the context's first stream).
+ * given CUDA stream (a cudaStream_t; NULL is the legacy default stream).
  * Returns after the work is enqueued; the caller synchronises the stream.
  * No reference counterpart: it is the device-pointer entry of the tile
  * kernel that src/Tiled-MM/tiled_mm.cpp:200-217 reaches through cuBLAS. */

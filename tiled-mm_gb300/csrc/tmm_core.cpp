@@ -161,6 +161,10 @@ int pin_range(tmm_context* ctx, const void* p, size_t bytes, Pin* out) {
   out->ptr = nullptr;
   out->owned = false;
   if (!p || bytes == 0) return TMM_SUCCESS;
+  // page-locked already (cudaHostAlloc / cudaMallocHost / an earlier registration): use as is
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeHost) return TMM_SUCCESS;
+  cudaGetLastError();
   cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
   if (e == cudaSuccess) {
     out->ptr = const_cast<void*>(p);
@@ -778,7 +782,7 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
   if (m == 0 || n == 0) return TMM_SUCCESS;
   if ((k > 0 && (!a || !b)) || !c) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: null matrix pointer");
   DeviceGuard dg(ctx->device);
-  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->streams[0];
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream, as everywhere in CUDA
   if (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE && k > 0) {
     // split op(A) and op(B) in k-tiles of at most tile_k (per-k-tile scaling) into scratch, then multiply
     const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
