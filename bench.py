@@ -155,6 +155,7 @@ def calibrate_slices(tmm, torch, w, native_metric_ref: float | None, log) -> tup
     tmm.fill_device(b.data_ptr(), k, n, k, w["kind"], w["param"], seed=101, mat_id=1)
     a_h, b_h = a.cpu().numpy(), b.cpu().numpy()
     ctx = tmm.make_context(np.float64, 1, 32768, 32768, 32768)
+    ctx.set_ozaki_engine(w["engine"])
     c = torch.zeros(m * n, dtype=torch.float64, device=dev)
     tmm.gemm_device(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m, stream=torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
@@ -214,6 +215,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     ctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
     if slices:
         ctx.set_path(tmm.PATH_OZAKI, slices)
+        ctx.set_ozaki_engine(w["engine"])
+    eng = ctx.ozaki_engine()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
     def dev_step():
@@ -286,6 +289,7 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     hctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
     if slices:
         hctx.set_path(tmm.PATH_OZAKI, slices)
+        hctx.set_ozaki_engine(w["engine"])
     e2e_times = []
     for it in range(max(1, args.e2e_warmup) + args.e2e_steps):
         pc.array[:] = 0.0
@@ -306,16 +310,22 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     for p in (pa, pb, pc):
         p.free()
 
-    eng = tmm.ozaki_engine()
     if w["path"] == "ozaki":
         pairs = slices * (slices + 1) // 2
         lowp_ops = pairs * flops
-        peak = MEASURED_ENGINE_PEAKS["imma_s8_tops"] if eng["engine"] == "imma" else None
+        if eng["engine"] == "imma":
+            peak = MEASURED_ENGINE_PEAKS["imma_s8_tops"]
+            src = "measured on this pool's GB300 by the repository's mma.sync s8 probe"
+        else:
+            bf16 = measured_peaks().get("bf16_tflops") or 1910.1
+            peak = 2.0 * bf16
+            src = "2 x the measured dense bf16 cuBLAS burst rate in MEASURED_PEAKS.json (e4m3 issues at twice bf16)"
         achieved = lowp_ops / t_step / 1e12
         result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                              "frac": (achieved / peak) if peak else None, "traffic": None,
-                              "kernel": f"oz_gemm_{eng['engine']}", "ops": f"{pairs} slice-pair products x 2mnk",
-                              "peak_source": "measured on this pool's GB300 by the repository's mma.sync probe"}
+                              "frac": achieved / peak, "traffic": None,
+                              "kernel": "oz_gemm_tc" if eng["engine"] == "tcgen05" else "oz_gemm_imma",
+                              "ops": f"{pairs} slice-pair products x 2mnk (whole step incl. split kernels)",
+                              "peak_source": src}
         result["slices"] = slices
         result["slice_pairs"] = pairs
         result["engine"] = eng
@@ -366,13 +376,14 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ozaki32768", choices=sorted(WORKLOADS))
     ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--engine", default="tcgen05", choices=["tcgen05", "imma"])
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--skip-native", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--e2e-warmup", type=int, default=1)
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload], engine=args.engine)
     rank, world, local, dist = dist_setup(args.gpus)
     log = (lambda s: print(s, file=sys.stderr, flush=True)) if rank == 0 else (lambda s: None)
     config = {"workload": w["desc"], "m": w["m"], "n": w["n"], "k": w["k"], "trans": w["ta"] + w["tb"],

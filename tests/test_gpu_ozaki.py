@@ -14,24 +14,49 @@ pytestmark = pytest.mark.gpu
 GOLDEN = np.load(Path(__file__).parent / "golden" / "reference_host_golden.npz")
 
 
-def ozaki_ctx(tmm, slices, tiles=(4096, 4096, 4096), streams=2):
+ENGINES = ["imma", "tcgen05"]
+
+
+def ozaki_ctx(tmm, slices, tiles=(4096, 4096, 4096), streams=2, engine="tcgen05"):
     ctx = tmm.make_context(np.float64, streams, *tiles)
     ctx.set_path(tmm.PATH_OZAKI, slices)
+    ctx.set_ozaki_engine(engine)
     return ctx
 
 
+@pytest.mark.parametrize("engine", ENGINES)
+def test_exact_accumulation_at_the_pass_limit(tmm, engine):
+    """Integers in [-15, 15] are one exact digit each; at k = 65536 the per-pass sums reach
+    15 * 15 * 65536 < 2^24, the limit of exact FP32 accumulation: the product must be exact."""
+    rng = np.random.default_rng(21)
+    m, n, k = 256, 256, 65536
+    a = rng.integers(-15, 16, m * k).astype(np.float64)
+    b = rng.integers(-15, 16, k * n).astype(np.float64)
+    a[: m * 512] = 15.0  # long runs of maximal products
+    b[: 512] = 15.0
+    c = np.zeros(m * n)
+    ctx = ozaki_ctx(tmm, 1, (65536, 65536, 65536), 1, engine)
+    tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)
+    A = a.reshape(k, m).T.astype(np.int64)
+    B = b.reshape(n, k).T.astype(np.int64)
+    want = (A @ B).astype(np.float64)
+    np.testing.assert_array_equal(c.reshape(n, m).T, want)
+
+
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("trans", ["NN", "NT", "TN", "TT"])
 @pytest.mark.parametrize("shape,tiles", [((129, 77, 200), (4096, 4096, 4096)),
                                          ((300, 260, 517), (128, 256, 128)),
-                                         ((64, 1, 33), (4096, 4096, 4096))])
-def test_bit_exact_vs_oracle(tmm, oracle, trans, shape, tiles):
+                                         ((64, 1, 33), (4096, 4096, 4096)),
+                                         ((700, 530, 1100), (512, 512, 1024))])
+def test_bit_exact_vs_oracle(tmm, oracle, engine, trans, shape, tiles):
     m, n, k = shape
     ta, tb = trans
-    eng = tmm.ozaki_engine()
     rng = np.random.default_rng(abs(hash((trans, shape))) % 2**32)
     a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, pad=3, kind="uexp")
     slices = 7
-    ctx = ozaki_ctx(tmm, slices, tiles)
+    ctx = ozaki_ctx(tmm, slices, tiles, engine=engine)
+    eng = ctx.ozaki_engine()
     out = c.copy()
     tmm.gemm(ctx, ta, tb, m, n, k, 0.75, a, lda, b, ldb, -1.25, out, ldc)
     tm, tn, tk = reference_tiles(oracle, m, n, k, tiles)
@@ -41,9 +66,10 @@ def test_bit_exact_vs_oracle(tmm, oracle, trans, shape, tiles):
     np.testing.assert_array_equal(out, want)
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("name", ["ci_small_tiles", "ci_smaller_than_tile", "beta_one", "beta_alpha", "tn", "nt",
                                   "tt", "default_tiles", "tn_short_k_tile"])
-def test_reference_known_answers_exact(tmm, name):
+def test_reference_known_answers_exact(tmm, engine, name):
     """Integer inputs are represented exactly by one slice: the emulated product is exact."""
     p = GOLDEN[f"{name}/params"]
     m, n, k, ta, tb = int(p[0]), int(p[1]), int(p[2]), chr(p[3]), chr(p[4])
@@ -53,7 +79,7 @@ def test_reference_known_answers_exact(tmm, name):
     a = GOLDEN[f"{name}/a"].astype(np.float64)
     b = GOLDEN[f"{name}/b"].astype(np.float64)
     c = GOLDEN[f"{name}/c"].astype(np.float64)
-    ctx = ozaki_ctx(tmm, 3, (tm, tn, tk), streams)
+    ctx = ozaki_ctx(tmm, 3, (tm, tn, tk), streams, engine)
     out = c.copy()
     tmm.gemm(ctx, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, out, ldc)
     np.testing.assert_array_equal(dense(out, ldc, m, n), exact_product(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta,
@@ -62,8 +88,9 @@ def test_reference_known_answers_exact(tmm, name):
         np.testing.assert_array_equal(out, GOLDEN[f"{name}/c_copy_back"])
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("kind", ["uniform", "uexp"])
-def test_error_within_native_bound(tmm, oracle, kind):
+def test_error_within_native_bound(tmm, oracle, engine, kind):
     rng = np.random.default_rng(11)
     m, n, k = 256, 192, 1024
     a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind=kind)
@@ -80,7 +107,7 @@ def test_error_within_native_bound(tmm, oracle, kind):
     e_native = metric(cn)
     errs = {}
     for s in (4, 8, 11, 13, 16):
-        ctx = ozaki_ctx(tmm, s)
+        ctx = ozaki_ctx(tmm, s, engine=engine)
         co = c.copy()
         tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.0, co, ldc)
         errs[s] = metric(co)
@@ -89,12 +116,13 @@ def test_error_within_native_bound(tmm, oracle, kind):
     assert e_native < 1.0
 
 
-def test_device_entry_matches_host_entry(tmm):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_device_entry_matches_host_entry(tmm, engine):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(12)
     m, n, k = 200, 300, 400
     a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k, kind="uexp")
-    ctx = ozaki_ctx(tmm, 9, (4096, 4096, 4096))
+    ctx = ozaki_ctx(tmm, 9, (4096, 4096, 4096), engine=engine)
     host = c.copy()
     tmm.gemm(ctx, "T", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, host, ldc)
     da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
@@ -104,13 +132,14 @@ def test_device_entry_matches_host_entry(tmm):
     np.testing.assert_array_equal(dc.cpu().numpy(), host)
 
 
-def test_out_of_core_ozaki_matches_in_core(tmm):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_out_of_core_ozaki_matches_in_core(tmm, engine):
     rng = np.random.default_rng(13)
     m, n, k = 512, 384, 640
     a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind="uexp")
-    big = ozaki_ctx(tmm, 8, (128, 128, 128))
-    small = ozaki_ctx(tmm, 8, (128, 128, 128))
-    small.set_memory_limit(2 * 1024 * 1024)  # forces A/B tile eviction
+    big = ozaki_ctx(tmm, 8, (128, 128, 128), engine=engine)
+    small = ozaki_ctx(tmm, 8, (128, 128, 128), engine=engine)
+    small.set_memory_limit(100 * 1024 * 1024)  # forces A/B tile eviction (the tcgen05 workspace is 37 MB/stream)
     o1, o2 = c.copy(), c.copy()
     tmm.gemm(big, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, o1, ldc)
     tmm.gemm(small, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, o2, ldc)

@@ -82,6 +82,8 @@ struct tmm_context {
   cudaStream_t d2h = nullptr;         // result stream (src/Tiled-MM/gpu_context.hpp:39)
 
   tmm::GrowBuffer pool_a, pool_b, pool_c, full_c, staging, scratch;
+  tmm::GrowBuffer oz_work;  // [256-byte error word block][per-stream FP64 workspaces of the tcgen05 engine]
+  int oz_engine = 0;
   tmm::TileCache cache_a, cache_b;
   std::vector<tmm::CSlot> cslots;  // 2 per stream
   std::vector<cudaEvent_t> staging_free;

@@ -231,6 +231,7 @@ extern "C" int tmm_create(int dtype, int n_streams, int max_tile_m, int max_tile
   ctx->max_tile_m = max_tile_m;
   ctx->max_tile_n = max_tile_n;
   ctx->max_tile_k = max_tile_k;
+  ctx->oz_engine = tmm::ozaki_default_engine();
   cudaError_t e = cudaGetDevice(&ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->prep, cudaStreamNonBlocking);
@@ -268,6 +269,7 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   ctx->full_c.release();
   ctx->staging.release();
   ctx->scratch.release();
+  ctx->oz_work.release();
   for (auto s : ctx->streams) cudaStreamDestroy(s);
   if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
   if (ctx->prep) cudaStreamDestroy(ctx->prep);
@@ -364,11 +366,19 @@ extern "C" int tmm_get_path(tmm_context* ctx, int* path, int* slices) {
   return TMM_SUCCESS;
 }
 
-extern "C" int tmm_get_ozaki_engine(int* engine, int* k_block, int64_t* pass_blocks) {
-  if (!engine || !k_block || !pass_blocks) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_ozaki_engine: null argument");
-  *engine = tmm::ozaki_engine();
-  *k_block = (int)tmm::ozaki_k_block();
-  *pass_blocks = tmm::ozaki_pass_blocks();
+extern "C" int tmm_set_ozaki_engine(tmm_context* ctx, int engine) {
+  if (!ctx || (engine != tmm::OZ_ENGINE_IMMA && engine != tmm::OZ_ENGINE_TCGEN05))
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_ozaki_engine: unknown engine");
+  ctx->oz_engine = engine;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_ozaki_engine(tmm_context* ctx, int* engine, int* k_block, int64_t* pass_blocks) {
+  if (!ctx || !engine || !k_block || !pass_blocks)
+    return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_ozaki_engine: null argument");
+  *engine = ctx->oz_engine;
+  *k_block = (int)tmm::ozaki_k_block(ctx->oz_engine);
+  *pass_blocks = tmm::ozaki_pass_blocks(ctx->oz_engine);
   return TMM_SUCCESS;
 }
 
@@ -418,8 +428,37 @@ extern "C" int tmm_get_full_c(tmm_context* ctx, void** ptr, size_t* size, size_t
 // ------------------------------------------------------------------ the pipeline
 namespace {
 
+// The tcgen05 engine's error word and per-stream FP64 workspaces.
+constexpr size_t OZ_ERR_BLOCK = 256;
+int reserve_oz_work(tmm_context* ctx, int streams) {
+  if (ctx->oz_engine != tmm::OZ_ENGINE_TCGEN05) return TMM_SUCCESS;
+  size_t per = (tmm::ozaki_workspace_bytes(ctx->oz_engine) + 255) / 256 * 256;
+  bool fresh = ctx->oz_work.ptr == nullptr;
+  TMM_CUDA(ctx, ctx->oz_work.reserve(OZ_ERR_BLOCK + (size_t)streams * per));
+  if (fresh || ctx->oz_work.bytes) TMM_CUDA(ctx, cudaMemset(ctx->oz_work.ptr, 0, OZ_ERR_BLOCK));
+  return TMM_SUCCESS;
+}
+double* oz_workspace(tmm_context* ctx, int stream_index) {
+  if (!ctx->oz_work.ptr) return nullptr;
+  size_t per = (tmm::ozaki_workspace_bytes(ctx->oz_engine) + 255) / 256 * 256;
+  return (double*)((char*)ctx->oz_work.ptr + OZ_ERR_BLOCK + (size_t)stream_index * per);
+}
+int* oz_error_word(tmm_context* ctx) { return ctx->oz_work.ptr ? (int*)ctx->oz_work.ptr : nullptr; }
+// after synchronisation: a bounded device wait that gave up
+int check_oz_error(tmm_context* ctx) {
+  if (!ctx->oz_work.ptr || ctx->oz_engine != tmm::OZ_ENGINE_TCGEN05) return TMM_SUCCESS;
+  int word = 0;
+  TMM_CUDA(ctx, cudaMemcpy(&word, ctx->oz_work.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (word) {
+    cudaMemset(ctx->oz_work.ptr, 0, OZ_ERR_BLOCK);
+    return fail(ctx, TMM_ERROR_TIMEOUT, "tcgen05 Ozaki kernel: a pipeline wait timed out");
+  }
+  return TMM_SUCCESS;
+}
+
 struct Plan {
   int64_t m, n, k, tm, tn, tk;
+  int engine;
   int64_t ntm, ntn, ntk;
   Op opa, opb;
   size_t es;
@@ -521,7 +560,7 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
     int64_t lines = lines_are_rows ? rr : cc;   // stored orientation resolved by caller
     int64_t kk = lines_are_rows ? cc : rr;
     Op t = lines_are_rows ? tmm::OP_N : tmm::OP_T;
-    tmm::OzakiSplit v = tmm::ozaki_split_view(s.ptr, lines, kk, P.slices);
+    tmm::OzakiSplit v = tmm::ozaki_split_view(s.ptr, lines, kk, P.slices, P.engine);
     cudaError_t e = tmm::ozaki_split((const double*)stage, rr, t, lines, kk, v, ctx->prep);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki split launch");
     ctx->stats.kernels++;
@@ -553,6 +592,8 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
     if (st) return st;
   }
   if (P.ozaki) {
+    st = reserve_oz_work(ctx, ns);
+    if (st) return st;
     size_t sb = (P.staging_bytes + 255) / 256 * 256;
     TMM_CUDA(ctx, ctx->staging.reserve(3 * sb));
     while (ctx->staging_free.size() < 3) {
@@ -643,10 +684,10 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
           st = launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s);
           if (st) return st;
         } else {
-          tmm::OzakiSplit va = tmm::ozaki_split_view(SA.ptr, mi, kk, P.slices);
-          tmm::OzakiSplit vb = tmm::ozaki_split_view(SB.ptr, nj, kk, P.slices);
+          tmm::OzakiSplit va = tmm::ozaki_split_view(SA.ptr, mi, kk, P.slices, P.engine);
+          tmm::OzakiSplit vb = tmm::ozaki_split_view(SB.ptr, nj, kk, P.slices, P.engine);
           cudaError_t e = tmm::ozaki_gemm(va, vb, mi, nj, *(const double*)alpha, *(const double*)beta, kt == 0,
-                                          (double*)ct, ldct, s);
+                                          (double*)ct, ldct, P.engine, oz_workspace(ctx, sidx), oz_error_word(ctx), s);
           if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki gemm launch");
           ctx->stats.kernels++;
         }
@@ -728,6 +769,7 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   P.es = elem_size(ctx->dtype);
   P.ozaki = ozaki;
   P.slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+  P.engine = ctx->oz_engine;
   if (ozaki) {
     P.a_slot_bytes = tmm::ozaki_split_bytes(tm, tk, P.slices);
     P.b_slot_bytes = tmm::ozaki_split_bytes(tn, tk, P.slices);
@@ -759,6 +801,7 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   if (!st) st = run_gemm(ctx, P, alpha, a, ld_a, b, ld_b, beta, c, ld_c, copy_c_back != 0);
   int st2 = sync_all(ctx);  // returns with C final (the reference syncs the device: tiled_mm.cpp:602-604)
   if (!st) st = st2;
+  if (!st && ozaki) st = check_oz_error(ctx);
   unpin(pa);
   unpin(pb);
   unpin(pc);
@@ -790,16 +833,19 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
     const size_t sa = tmm::ozaki_split_bytes(m, tk, slices), sb = tmm::ozaki_split_bytes(n, tk, slices);
     const size_t sa_al = (sa + 255) / 256 * 256;
     TMM_CUDA(ctx, ctx->scratch.reserve(sa_al + sb));
+    int st = reserve_oz_work(ctx, 1);
+    if (st) return st;
     for (int64_t k0 = 0, kt = 0; k0 < k; k0 += tk, ++kt) {
       const int64_t kk = std::min(tk, k - k0);
-      tmm::OzakiSplit va = tmm::ozaki_split_view(ctx->scratch.ptr, m, kk, slices);
-      tmm::OzakiSplit vb = tmm::ozaki_split_view((char*)ctx->scratch.ptr + sa_al, n, kk, slices);
+      tmm::OzakiSplit va = tmm::ozaki_split_view(ctx->scratch.ptr, m, kk, slices, ctx->oz_engine);
+      tmm::OzakiSplit vb = tmm::ozaki_split_view((char*)ctx->scratch.ptr + sa_al, n, kk, slices, ctx->oz_engine);
       const double* ab = opa == tmm::OP_N ? (const double*)a + k0 * ld_a : (const double*)a + k0;
       const double* bb = opb == tmm::OP_N ? (const double*)b + k0 : (const double*)b + k0 * ld_b;
       cudaError_t e = tmm::ozaki_split(ab, ld_a, opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, m, kk, va, s);
       if (e == cudaSuccess) e = tmm::ozaki_split(bb, ld_b, opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, n, kk, vb, s);
       if (e == cudaSuccess)
-        e = tmm::ozaki_gemm(va, vb, m, n, *(const double*)alpha, *(const double*)beta, kt == 0, (double*)c, ld_c, s);
+        e = tmm::ozaki_gemm(va, vb, m, n, *(const double*)alpha, *(const double*)beta, kt == 0, (double*)c, ld_c,
+                            ctx->oz_engine, oz_workspace(ctx, 0), oz_error_word(ctx), s);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki device gemm launch");
       ctx->stats.kernels += 3;
     }

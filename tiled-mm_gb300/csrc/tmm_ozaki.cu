@@ -32,17 +32,12 @@
 namespace tmm {
 
 // ------------------------------------------------------------------ configuration
-int ozaki_engine() {
-  static int engine = [] {
-    const char* e = getenv("TMM_OZAKI_ENGINE");
-    if (e && strcmp(e, "imma") == 0) return (int)OZ_ENGINE_IMMA;
-    if (e && strcmp(e, "tcgen05") == 0) return (int)OZ_ENGINE_TCGEN05;
-    return (int)OZ_ENGINE_IMMA;
-  }();
-  return engine;
+int ozaki_default_engine() {
+  const char* e = getenv("TMM_OZAKI_ENGINE");
+  if (e && strcmp(e, "imma") == 0) return OZ_ENGINE_IMMA;
+  if (e && strcmp(e, "tcgen05") == 0) return OZ_ENGINE_TCGEN05;
+  return OZ_ENGINE_IMMA;
 }
-
-int ozaki_encoding() { return ozaki_engine() == OZ_ENGINE_TCGEN05 ? OZ_ENC_E4M3 : OZ_ENC_INT8; }
 
 size_t ozaki_split_bytes(int64_t rows, int64_t kk, int slices) {
   int64_t rp = oz_round_up(rows > 0 ? rows : 1, OZ_ROW_ALIGN);
@@ -52,14 +47,14 @@ size_t ozaki_split_bytes(int64_t rows, int64_t kk, int slices) {
   return digits + (size_t)rp * sizeof(int32_t);
 }
 
-OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices) {
+OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices, int engine) {
   OzakiSplit v;
   v.rows = rows;
   v.kk = kk;
   v.rows_pad = oz_round_up(rows > 0 ? rows : 1, OZ_ROW_ALIGN);
   v.k_pad = oz_round_up(kk > 0 ? kk : 1, OZ_K_ALIGN);
   v.slices = slices;
-  v.enc = ozaki_encoding();
+  v.enc = ozaki_encoding(engine);
   size_t digits = (size_t)slices * (size_t)v.rows_pad * (size_t)v.k_pad;
   digits = (digits + 1023) / 1024 * 1024;
   v.digits = (uint8_t*)base;
@@ -321,8 +316,9 @@ oz_gemm_imma(const uint8_t* __restrict__ Ad, const int32_t* __restrict__ ea, int
 
 }  // namespace
 
-int64_t ozaki_pass_blocks() { return IM_PASS_BLOCKS; }
-int64_t ozaki_k_block() { return IM_KB; }
+int64_t ozaki_pass_blocks(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_pass_blocks() : IM_PASS_BLOCKS; }
+int64_t ozaki_k_block(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_k_block() : IM_KB; }
+size_t ozaki_workspace_bytes(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_workspace_bytes() : 0; }
 
 cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int64_t kk, const OzakiSplit& out,
                         cudaStream_t s) {
@@ -338,8 +334,10 @@ cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int
 }
 
 cudaError_t ozaki_gemm(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
-                       bool first_k_tile, double* C, int64_t ldc, cudaStream_t s) {
+                       bool first_k_tile, double* C, int64_t ldc, int engine, double* work, int* err, cudaStream_t s) {
   if (m <= 0 || n <= 0) return cudaSuccess;
+  if (engine == OZ_ENGINE_TCGEN05) return ozaki_gemm_tc(A, B, m, n, alpha, beta, first_k_tile, C, ldc, work, err, s);
+  if (A.enc != OZ_ENC_INT8 || B.enc != OZ_ENC_INT8) return cudaErrorInvalidValue;
   if (A.k_pad != B.k_pad || A.slices != B.slices || A.rows_pad < m || B.rows_pad < n) return cudaErrorInvalidValue;
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;

@@ -14,7 +14,7 @@
 
 namespace tmm {
 
-constexpr int OZ_ROW_ALIGN = 128;  // lines are padded to the GEMM tile
+constexpr int OZ_ROW_ALIGN = 256;  // lines are padded to the GEMM tiles (128 x 256)
 constexpr int OZ_K_ALIGN = 128;    // k is padded to whole k-blocks (bytes)
 constexpr int OZ_DIGIT_BITS = 5;   // |d| <= 2^(w-1) = 16: exact in int8 and in e4m3
 constexpr int OZ_MAX_SLICES = 20;
@@ -35,14 +35,14 @@ struct OzakiSplit {
 
 inline int64_t oz_round_up(int64_t v, int64_t q) { return (v + q - 1) / q * q; }
 
-// the engine used by ozaki_split/ozaki_gemm (environment TMM_OZAKI_ENGINE=imma|tcgen05)
-int ozaki_engine();
-int ozaki_encoding();
+// default engine of new contexts (environment TMM_OZAKI_ENGINE=imma|tcgen05 overrides)
+int ozaki_default_engine();
+inline int ozaki_encoding(int engine) { return engine == OZ_ENGINE_TCGEN05 ? OZ_ENC_E4M3 : OZ_ENC_INT8; }
 
 // bytes needed by a split tile of rows x kk
 size_t ozaki_split_bytes(int64_t rows, int64_t kk, int slices);
-// lay out a split tile in a buffer of ozaki_split_bytes bytes (encoding of the current engine)
-OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices);
+// lay out a split tile in a buffer of ozaki_split_bytes bytes, digits encoded for `engine`
+OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices, int engine);
 
 // Split `rows` lines of a device FP64 operand into `out`:
 //   trans == OP_N: line r, element l = X[r + l * ld];   otherwise X[l + r * ld].
@@ -51,11 +51,22 @@ cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int
 
 // C (m x n, ldc) = alpha * A_split * B_split^T + beta' * C, beta' = beta on the
 // first k-tile (C not read when beta == 0) and 1 afterwards.
+// work: ozaki_workspace_bytes(engine) of device memory private to this launch; err: a device
+// word that a timed-out wait sets (tcgen05 engine).
 cudaError_t ozaki_gemm(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha,
-                       double beta, bool first_k_tile, double* C, int64_t ldc, cudaStream_t s);
+                       double beta, bool first_k_tile, double* C, int64_t ldc, int engine, double* work, int* err,
+                       cudaStream_t s);
 
+size_t ozaki_workspace_bytes(int engine);
 // k-blocks (of the engine's k-block size) accumulated between two FP64 drains
-int64_t ozaki_pass_blocks();
-int64_t ozaki_k_block();
+int64_t ozaki_pass_blocks(int engine);
+int64_t ozaki_k_block(int engine);
+
+// tcgen05 engine (tmm_tcgen05.cu)
+size_t ozaki_tc_workspace_bytes();
+int64_t ozaki_tc_pass_blocks();
+int ozaki_tc_k_block();
+cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
+                          bool first_k_tile, double* C, int64_t ldc, double* work, int* err, cudaStream_t s);
 
 }  // namespace tmm

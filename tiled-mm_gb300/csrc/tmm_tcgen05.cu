@@ -1,0 +1,457 @@
+// tcgen05 engine of the Ozaki path: exact e4m3 digit-plane products on the
+// 5th-generation tensor cores of sm_103a, FP64 recombination, fused epilogue.
+//
+// Per CTA (persistent, one per SM) output tiles of 128 x 256:
+//   warp 0      TMA producer: 128 x 128-byte A and 256 x 128-byte B digit
+//               tiles (SWIZZLE_128B) into a 4-stage shared-memory ring
+//               (full/empty mbarriers, expect_tx byte counts);
+//   warp 1      allocates 512 TMEM columns and, from one thread, issues
+//               tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256, K=32)
+//               into one of two 256-column FP32 accumulators, committing
+//               stage releases and "accumulator full" to mbarriers;
+//   warps 2-5   drain a full accumulator with tcgen05.ld (one TMEM lane per
+//               thread), release it, and add 2^(-5 g) * S to the tile's FP64
+//               accumulator in a per-CTA workspace slot (L2-resident, each
+//               thread owns its elements); after the tile's last pass they
+//               apply 2^(e_i + f_j - 8), alpha and beta and store C.
+// The sequence of (diagonal g, slice pair p, k-block) and the exactness
+// passes (at most OZ_TC_PASS_BLOCKS k-blocks of 128: 65536 products of
+// |d_a d_b| <= 256 stay below 2^24, exact in FP32) is the one the oracle
+// (oracle/tmm_ozaki_oracle.c) replays.  Every mbarrier wait is bounded: after
+// about a second it records an error word and the CTA winds down (waiting,
+// again bounded, for its copies and MMAs in flight) and frees its TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "tmm_ozaki.h"
+
+namespace tmm {
+namespace tc {
+
+constexpr int BM = 128, BN = 256, KB = 128;  // KB: bytes (= e4m3 elements) per k-block
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * KB, B_BYTES = BN * KB, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int THREADS = 192;
+constexpr int TMEM_COLS = 512;
+constexpr int64_t PASS_BLOCKS = 512;  // 512 * 128 = 65536 k terms per exact FP32 pass
+constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+constexpr unsigned long long WAIT_NS = 1000000000ull;  // one second per wait
+
+// ------------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false after WAIT_NS (error word set) or when another role gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err) {
+  for (int i = 0; i < 256; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicOr(err, 1);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t slot_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_smem), "r"(ncols));
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+// K-major operand, 128-byte swizzle, 8-row core groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                  // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+  return d;
+}
+
+// kind::f8f6f4: D f32, A e4m3, B e4m3, both K-major, N = 256, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ------------------------------------------------------------------ work sequence
+// Per tile: for g = s-1 .. 0, p = 0 .. g (q = g - p), kb = 0 .. nkb-1; a pass ends
+// after PASS_BLOCKS k-blocks or at the end of a diagonal.
+struct Seq {
+  int s, nkb;
+  int g, p, kb;
+  int64_t used;
+  __device__ void start(int s_, int nkb_) {
+    s = s_;
+    nkb = nkb_;
+    g = s - 1;
+    p = 0;
+    kb = 0;
+    used = 0;
+  }
+  __device__ bool done() const { return g < 0; }
+  __device__ bool pass_first() const { return used == 0; }
+  // true when the current k-block closes a pass
+  __device__ bool pass_last() const { return used + 1 == PASS_BLOCKS || (kb == nkb - 1 && p == g); }
+  __device__ void next() {
+    used = pass_last() ? 0 : used + 1;
+    if (++kb == nkb) {
+      kb = 0;
+      if (++p > g) {
+        p = 0;
+        --g;
+      }
+    }
+  }
+};
+
+struct Params {
+  const int32_t* ea;
+  const int32_t* eb;
+  int64_t a_rows_pad, b_rows_pad;
+  int nkb, s;
+  int64_t m, n;
+  double alpha, beta;
+  int first;
+  double* C;
+  int64_t ldc;
+  double* work;  // gridDim.x slots of BM * BN doubles
+  int* err;
+  int tiles_m, tiles_n;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + (size_t)STAGES * STAGE_BYTES);
+  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2]
+  volatile int* abort_flag = (volatile int*)(bars + 2 * STAGES + 4);
+  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+  const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
+  const int total_tiles = P.tiles_m * P.tiles_n;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(full0 + 8 * i, 1);
+      mbar_init(empty0 + 8 * i, 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(tfull0 + 8 * i, 1);
+      mbar_init(tempty0 + 8 * i, 4);  // one arrival per epilogue warp
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0 && lane == 0) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == 1) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- TMA producer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+        const int tm = tile % P.tiles_m, tn = tile / P.tiles_m;
+        Seq q;
+        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+          ok = mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
+          if (!ok) break;
+          const uint32_t fb = full0 + 8 * stage;
+          mbar_expect_tx(fb, STAGE_BYTES);
+          uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
+          tma_load_2d(smem_u32(sa), &tmA, q.kb * KB, (int)(q.p * P.a_rows_pad + (int64_t)tm * BM), fb);
+          tma_load_2d(smem_u32(sa + A_BYTES), &tmB, q.kb * KB, (int)((q.g - q.p) * P.b_rows_pad + (int64_t)tn * BN), fb);
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // drain: every issued copy has landed before the CTA may exit (bounded)
+      for (int i = 0; i < STAGES; ++i) {
+        (void)mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
+        if (++stage == STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t tphase[2] = {0, 0};
+      int buf = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+        Seq q;
+        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+          if (q.pass_first()) {
+            ok = mbar_wait(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, P.err);
+            if (!ok) break;
+            tc_fence_after();
+          }
+          ok = mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + (size_t)stage * STAGE_BYTES);
+          const uint64_t ad = smem_desc(sa), bd = smem_desc(sa + A_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < KB / 32; ++kk)  // K = 32 e4m3 = 32 bytes per MMA: +2 in the 16-byte address field
+            mma_f8(d_tmem, ad + 2 * kk, bd + 2 * kk, (q.pass_first() && kk == 0) ? 0u : 1u);
+          mma_commit(empty0 + 8 * stage);  // the stage is free when these MMAs have read it
+          if (q.pass_last()) {
+            mma_commit(tfull0 + 8 * buf);
+            tphase[buf] ^= 1;
+            buf ^= 1;
+          }
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // wait (bounded) for the MMAs in flight before TMEM is freed
+      for (int b = 0; b < 2; ++b) {
+        (void)mbar_wait(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, P.err);
+        buf ^= 1;
+      }
+    }
+  } else {
+    // ---------------------------------------------------------------- epilogue (warps 2..5)
+    const int quarter = warp & 3;        // TMEM lanes 32*quarter .. +31 are this warp's
+    const int row = quarter * 32 + lane;  // tile row = TMEM lane
+    double* slot = P.work + (size_t)blockIdx.x * (size_t)(BM * BN);
+    uint32_t tphase[2] = {0, 0};
+    int buf = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+      const int tm = tile % P.tiles_m, tn = tile / P.tiles_m;
+      bool first_pass = true;
+      Seq q;
+      for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+        if (!q.pass_last()) continue;
+        // one lane waits, the warp follows: the TMEM loads below are warp-collective
+        int okw = 1;
+        if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+        __syncwarp();
+        if (!ok) break;
+        tc_fence_after();
+        const double wg = scalbn(1.0, -OZ_DIGIT_BITS * q.g);
+        const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
+#pragma unroll 1
+        for (int c = 0; c < BN / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tbase + (uint32_t)(c * 32), r);
+          tmem_ld_wait();
+          if (c == BN / 32 - 1) {  // accumulator consumed: hand it back to the MMA warp
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            double* w = slot + (size_t)(c * 32 + j) * BM + row;
+            const double v = (double)__uint_as_float(r[j]);
+            *w = (first_pass ? 0.0 : *w) + wg * v;
+          }
+        }
+        first_pass = false;
+        tphase[buf] ^= 1;
+        buf ^= 1;
+      }
+      if (!ok) break;
+      // fused epilogue: C = alpha * 2^(e_i + f_j - 8) * acc + beta' * C
+      const int64_t gi = (int64_t)tm * BM + row;
+      if (gi < P.m) {
+        const int ei = P.ea[gi];
+        for (int col = 0; col < BN; ++col) {
+          const int64_t gj = (int64_t)tn * BN + col;
+          if (gj >= P.n) break;
+          const double t = scalbn(slot[(size_t)col * BM + row], ei + P.eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
+          double* cp = P.C + gi + gj * P.ldc;
+          if (!P.first) *cp = fma(P.alpha, t, *cp);
+          else if (P.beta != 0.0) *cp = fma(P.alpha, t, P.beta * *cp);
+          else *cp = P.alpha * t;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem_base, TMEM_COLS);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+cudaError_t make_map(CUtensorMap* map, const OzakiSplit& X, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {(cuuint64_t)X.k_pad, (cuuint64_t)X.slices * (cuuint64_t)X.rows_pad};
+  cuuint64_t strides[1] = {(cuuint64_t)X.k_pad};
+  cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)X.digits, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+int num_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  });
+  return sms;
+}
+
+}  // namespace tc
+
+size_t ozaki_tc_workspace_bytes() { return (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
+int64_t ozaki_tc_pass_blocks() { return tc::PASS_BLOCKS; }
+int ozaki_tc_k_block() { return tc::KB; }
+
+cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
+                          bool first_k_tile, double* C, int64_t ldc, double* work, int* err, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  if (A.enc != OZ_ENC_E4M3 || B.enc != OZ_ENC_E4M3 || A.k_pad != B.k_pad || A.slices != B.slices ||
+      A.rows_pad % tc::BM || B.rows_pad % tc::BN || A.k_pad % tc::KB || !work || !err)
+    return cudaErrorInvalidValue;
+  // TMA coordinates are 32-bit: the stacked planes must stay addressable
+  if ((int64_t)A.slices * A.rows_pad > INT32_MAX || (int64_t)B.slices * B.rows_pad > INT32_MAX) return cudaErrorInvalidValue;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(tc::oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
+  });
+  if (attr != cudaSuccess) return attr;
+  CUtensorMap ma, mb;
+  cudaError_t e = tc::make_map(&ma, A, tc::BM);
+  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN);
+  if (e != cudaSuccess) return e;
+  tc::Params P;
+  P.ea = A.exps;
+  P.eb = B.exps;
+  P.a_rows_pad = A.rows_pad;
+  P.b_rows_pad = B.rows_pad;
+  P.nkb = (int)(A.k_pad / tc::KB);
+  P.s = A.slices;
+  P.m = m;
+  P.n = n;
+  P.alpha = alpha;
+  P.beta = beta;
+  P.first = first_k_tile ? 1 : 0;
+  P.C = C;
+  P.ldc = ldc;
+  P.work = work;
+  P.err = err;
+  P.tiles_m = (int)((m + tc::BM - 1) / tc::BM);
+  P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
+  int tiles = P.tiles_m * P.tiles_n;
+  int grid = tiles < tc::num_sms() ? tiles : tc::num_sms();
+  tc::oz_gemm_tc<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, P);
+  return cudaGetLastError();
+}
+
+}  // namespace tmm

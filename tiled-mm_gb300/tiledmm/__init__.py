@@ -35,6 +35,7 @@ _lib = C.CDLL(str(LIB_PATH))
 
 FLOAT, DOUBLE, COMPLEX_FLOAT, COMPLEX_DOUBLE = 0, 1, 2, 3
 PATH_NATIVE, PATH_OZAKI = 0, 1
+OZAKI_IMMA, OZAKI_TCGEN05 = 0, 1
 TILE_POLICY_REFERENCE, TILE_POLICY_FIXED, TILE_POLICY_AUTOTUNE = 0, 1, 2
 STATUS = {0: "success", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
           4: "not supported", 5: "internal error", 6: "device wait timed out"}
@@ -65,7 +66,8 @@ SIGNATURES = {
     "tmm_set_streams_and_tiles": (_ci, [_p, _ci, _ci, _ci, _ci]),
     "tmm_set_path": (_ci, [_p, _ci, _ci]),
     "tmm_get_path": (_ci, [_p, C.POINTER(_ci), C.POINTER(_ci)]),
-    "tmm_get_ozaki_engine": (_ci, [C.POINTER(_ci), C.POINTER(_ci), C.POINTER(_i64)]),
+    "tmm_set_ozaki_engine": (_ci, [_p, _ci]),
+    "tmm_get_ozaki_engine": (_ci, [_p, C.POINTER(_ci), C.POINTER(_ci), C.POINTER(_i64)]),
     "tmm_set_tile_policy": (_ci, [_p, _ci]),
     "tmm_set_memory_limit": (_ci, [_p, _sz]),
     "tmm_get_stats": (_ci, [_p, _p]),
@@ -231,6 +233,16 @@ class MMHandle:
         _check(_lib.tmm_get_path(self._h, C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
 
+    def set_ozaki_engine(self, engine) -> None:
+        e = {"imma": OZAKI_IMMA, "tcgen05": OZAKI_TCGEN05}.get(engine, engine)
+        _check(_lib.tmm_set_ozaki_engine(self._h, e), self._h)
+
+    def ozaki_engine(self) -> dict:
+        """Which engine runs the Ozaki slice products, its k-block and exactness pass length."""
+        e, kb, pb = _ci(), _ci(), _i64()
+        _check(_lib.tmm_get_ozaki_engine(self._h, C.byref(e), C.byref(kb), C.byref(pb)), self._h)
+        return {"engine": ["imma", "tcgen05"][e.value], "k_block": kb.value, "pass_blocks": pb.value}
+
     def set_tile_policy(self, policy: int) -> None:
         _check(_lib.tmm_set_tile_policy(self._h, policy), self._h)
 
@@ -272,13 +284,6 @@ def gemm_device(ctx: MMHandle, trans_a: str, trans_b: str, m: int, n: int, k: in
     st = _lib.tmm_gemm_device(ctx._h, trans_a.encode()[:1], trans_b.encode()[:1], m, n, k, al.ctypes.data, _ptr(a_dev),
                               ld_a, _ptr(b_dev), ld_b, be.ctypes.data, _ptr(c_dev), ld_c, stream)
     _check(st, ctx._h)
-
-
-def ozaki_engine() -> dict:
-    """Which engine runs the Ozaki slice products, its k-block and exactness pass length."""
-    e, kb, pb = _ci(), _ci(), _i64()
-    _check(_lib.tmm_get_ozaki_engine(C.byref(e), C.byref(kb), C.byref(pb)))
-    return {"engine": ["imma", "tcgen05"][e.value], "k_block": kb.value, "pass_blocks": pb.value}
 
 
 class PinnedArray:
