@@ -109,6 +109,25 @@ int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int
                     const void* alpha, const void* a_dev, int64_t ld_a, const void* b_dev, int64_t ld_b,
                     const void* beta, void* c_dev, int64_t ld_c, void* stream);
 
+/* No counterpart in the reference.  The Ozaki (emulated FP64) product on
+ * device operands for callers that cannot allocate device memory while they
+ * run -- a framework whose caching allocator already owns the GPU, or a
+ * latency-critical caller that cannot take cudaFree's device-wide sync.  It
+ * calls no cudaMalloc/cudaFree: its scratch is one fixed 96 MiB array of
+ * device memory inside the library, held by every GPU that loads the library
+ * until exit.  Up to slices * (round256(m) + round256(n)) * k_tile bytes of
+ * digits per k step fit (k_tile = 0 picks the largest that fits, a multiple of
+ * 128); larger requests fail with TMM_ERROR_INVALID_ARGUMENT and a message in
+ * tmm_last_error(NULL).  All calls share the array: calls that overlap on the
+ * GPU race.  The first call on a device looks up the array's device address;
+ * make it before any stream capture.  Enqueues on `stream` (NULL: legacy
+ * default stream) and returns; results equal tmm_gemm_device's with the
+ * tcgen05 engine, the same slice count and max_tile_k = k_tile. */
+int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                                  const double* a_dev, int64_t ld_a, const double* b_dev, int64_t ld_b,
+                                  double beta, double* c_dev, int64_t ld_c, int slices, int64_t k_tile,
+                                  void* stream);
+
 /* Replaces mm_handle::get_full_device_buffer_c() (src/Tiled-MM/mm_handle.cpp:162-165)
  * and its device_vector::data()/size()/capacity() (src/Tiled-MM/device_vector.hpp:67-80):
  * the device pointer of the compact (ld = m) result left by copy_c_back == 0. */

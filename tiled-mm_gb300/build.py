@@ -25,7 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", str(PKG.parent / "include"), "-I", str(CSRC)]
 
-SOURCES = ["tmm_core.cpp", "tmm_native.cu", "tmm_ozaki.cu", "tmm_tcgen05.cu", "tmm_batched.cu", "tmm_autotune.cpp"]
+SOURCES = ["tmm_core.cpp", "tmm_native.cu", "tmm_ozaki.cu", "tmm_tcgen05.cu", "tmm_batched.cu", "tmm_autotune.cpp",
+           "tmm_noalloc.cu"]
 LIB = OUT / "libtiledmm_gb300.so"
 CMP_LIB = OUT / "libtmm_cublas_cmp.so"
 

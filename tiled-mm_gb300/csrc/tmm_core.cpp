@@ -183,6 +183,8 @@ void unpin(Pin& p) {
 
 }  // namespace
 
+void tmm::set_last_error_message(const char* msg) { g_last_error = msg ? msg : ""; }
+
 // ------------------------------------------------------------------ GrowBuffer
 cudaError_t tmm::GrowBuffer::reserve(size_t want) {
   if (want <= capacity) {

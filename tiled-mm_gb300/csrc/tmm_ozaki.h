@@ -62,6 +62,9 @@ size_t ozaki_workspace_bytes(int engine);
 int64_t ozaki_pass_blocks(int engine);
 int64_t ozaki_k_block(int engine);
 
+// sets the message that tmm_last_error(NULL) returns on the calling thread (tmm_core.cpp)
+void set_last_error_message(const char* msg);
+
 // tcgen05 engine (tmm_tcgen05.cu)
 size_t ozaki_tc_workspace_bytes();
 int64_t ozaki_tc_pass_blocks();

@@ -55,6 +55,8 @@ SIGNATURES = {
     "tmm_destroy": (_ci, [_p]),
     "tmm_gemm": (_ci, [_p, C.c_char, C.c_char, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64, _ci, _ci]),
     "tmm_gemm_device": (_ci, [_p, C.c_char, C.c_char, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64, _p]),
+    "tmm_ozaki_gemm_device_noalloc": (_ci, [C.c_char, C.c_char, _i64, _i64, _i64, C.c_double, _p, _i64, _p, _i64,
+                                            C.c_double, _p, _i64, _ci, _i64, _p]),
     "tmm_get_full_c": (_ci, [_p, C.POINTER(_p), C.POINTER(_sz), C.POINTER(_sz)]),
     "tmm_set_num_streams": (_ci, [_p, _ci]),
     "tmm_get_num_streams": (_ci, [_p, C.POINTER(_ci)]),
