@@ -66,6 +66,25 @@ def test_bit_exact_vs_oracle(tmm, oracle, engine, trans, shape, tiles):
     np.testing.assert_array_equal(out, want)
 
 
+@pytest.mark.parametrize("cluster", ["1", "2", "4"])
+@pytest.mark.parametrize("shape", [(700, 530, 1100), (1100, 300, 700), (129, 600, 257)])
+def test_tcgen05_cluster_sizes_bit_exact(tmm, oracle, monkeypatch, cluster, shape):
+    """CTA clusters that share B tiles by multicast (forced sizes 1, 2, 4; row-tile
+    counts that leave padding tiles in the last cluster) give the oracle's bits."""
+    monkeypatch.setenv("TMM_TC_CLUSTER", cluster)
+    m, n, k = shape
+    rng = np.random.default_rng(m * 7 + n)
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k, pad=1, kind="uexp")
+    ctx = ozaki_ctx(tmm, 6, (4096, 4096, 512), engine="tcgen05")
+    out = c.copy()
+    tmm.gemm(ctx, "N", "T", m, n, k, 1.0, a, lda, b, ldb, 0.5, out, ldc)
+    eng = ctx.ozaki_engine()
+    tk = reference_tiles(oracle, m, n, k, (4096, 4096, 512))[2]
+    want = ozaki_oracle(oracle, "N", "T", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc, 6, tk, eng["k_block"],
+                        eng["pass_blocks"])
+    np.testing.assert_array_equal(out, want)
+
+
 @pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("name", ["ci_small_tiles", "ci_smaller_than_tile", "beta_one", "beta_alpha", "tn", "nt",
                                   "tt", "default_tiles", "tn_short_k_tile"])

@@ -75,59 +75,116 @@ __device__ __forceinline__ uint32_t digit_byte(int d, int enc) {
 }
 
 constexpr int SP_LINES = 32, SP_L = 64, SP_THREADS = 256;
+constexpr int SP_KCHUNK = 512;        // k elements per digit block
+constexpr int MX_LINES = 256, MX_KCHUNK = 256;
+constexpr int EXP_NONE = (int)0x80808080;  // "no nonzero element yet" (byte pattern of the clearing memset)
 
+// frexp exponent of |x| from its IEEE bits (x != 0): 2^(e-1) <= |x| < 2^e
+__device__ __forceinline__ int frexp_exponent_bits(uint64_t bits) {
+  const int eb = (int)((bits >> 52) & 0x7FF);
+  if (eb) return eb - 1022;
+  return -1010 - __clzll(bits & 0xFFFFFFFFFFFFFull);  // subnormal: -1074 + bit length
+}
+
+// Pass 1: line exponents.  Each thread folds the largest frexp exponent of its
+// line segment into exps[line] with one atomicMax (exps cleared to EXP_NONE).
 template <int TRANS>
 __global__ void __launch_bounds__(SP_THREADS)
-oz_split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, uint8_t* __restrict__ digits,
-                int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc) {
+oz_linemax_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, int32_t* __restrict__ exps) {
+  const int64_t k0 = (int64_t)blockIdx.y * MX_KCHUNK;
+  const int64_t k1 = k0 + MX_KCHUNK < kk ? k0 + MX_KCHUNK : kk;
+  if (TRANS == 0) {  // lines are contiguous across r: one line per thread, coalesced across the warp
+    const int64_t r = (int64_t)blockIdx.x * MX_LINES + threadIdx.x;
+    if (r >= rows) return;
+    uint64_t mx = 0;
+    for (int64_t l = k0; l < k1; ++l) {
+      const uint64_t b = (uint64_t)__double_as_longlong(X[r + l * ld]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+    if (mx) atomicMax(&exps[r], frexp_exponent_bits(mx));
+  } else {  // line r is contiguous along l: a warp per line segment
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t r = (int64_t)blockIdx.x * MX_LINES + w; r < (int64_t)(blockIdx.x + 1) * MX_LINES && r < rows; r += 8) {
+      uint64_t mx = 0;
+      for (int64_t l = k0 + lane; l < k1; l += 32) {
+        const uint64_t b = (uint64_t)__double_as_longlong(X[l + r * ld]) & 0x7FFFFFFFFFFFFFFFull;
+        mx = b > mx ? b : mx;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t v = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = v > mx ? v : mx;
+      }
+      if (lane == 0 && mx) atomicMax(&exps[r], frexp_exponent_bits(mx));
+    }
+  }
+}
+
+// One element's digits, exactly as the FP64 recurrence t = x 2^-e 16; d = rint(t);
+// t = (t - d) 32 computes them (every step of which is exact), emulated on the
+// integer pipes: x = m 2^E (53-bit m), t = r / 2^f with f = e - 4 - E fractional
+// bits, rint = round half to even on the integer r.
+struct DigitState {
+  int64_t r;
+  int f;
+  bool neg;
+  __device__ __forceinline__ void init(double x, int e) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(x);
+    neg = (bits >> 63) != 0;
+    const int eb = (int)((bits >> 52) & 0x7FF);
+    const uint64_t mant = bits & 0xFFFFFFFFFFFFFull;
+    r = (int64_t)(eb ? (mant | (1ull << 52)) : mant);
+    f = e - 4 - (eb ? eb - 1075 : -1074);
+  }
+  __device__ __forceinline__ int next() {
+    int64_t d;
+    if (f >= 63) {
+      d = 0;  // |t| < 2^53 / 2^63: rounds to 0, the remainder is unchanged
+    } else if (f > 0) {
+      const int64_t q = r >> f;  // floor
+      const int64_t frac = r - (q << f);
+      const int64_t half = (int64_t)1 << (f - 1);
+      d = q + ((frac > half || (frac == half && (q & 1))) ? 1 : 0);
+      r -= d << f;
+    } else {
+      d = r << (-f);  // t is an integer already
+      r = 0;
+    }
+    f -= OZ_DIGIT_BITS;
+    return neg ? -(int)d : (int)d;
+  }
+};
+
+// Pass 2: digits of 32 lines x SP_KCHUNK k per block, staged through shared
+// memory so both the FP64 reads and the byte writes are coalesced.
+template <int TRANS>
+__global__ void __launch_bounds__(SP_THREADS)
+oz_digits_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, uint8_t* __restrict__ digits,
+                 int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc) {
   __shared__ double tile[SP_LINES][SP_L + 1];
-  __shared__ double red[8][SP_LINES];
   __shared__ int sexp[SP_LINES];
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * SP_LINES;
-
-  // ---- phase 1: largest magnitude of each line
-  if (TRANS == 0) {
-    const int r = tid & 31, lg = tid >> 5;
-    double mx = 0.0;
-    if (r0 + r < rows)
-      for (int64_t l = lg; l < kk; l += 8) mx = fmax(mx, fabs(X[(r0 + r) + l * ld]));
-    red[lg][r] = mx;
-  } else {
-    const int lane = tid & 31, w = tid >> 5;
-    for (int rr = w; rr < SP_LINES; rr += 8) {
-      double mx = 0.0;
-      if (r0 + rr < rows)
-        for (int64_t l = lane; l < kk; l += 32) mx = fmax(mx, fabs(X[l + (r0 + rr) * ld]));
-      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (lane == 0) red[0][rr] = mx;
-    }
-  }
-  __syncthreads();
   if (tid < SP_LINES) {
-    double mx = red[0][tid];
-    if (TRANS == 0)
-      for (int q = 1; q < 8; ++q) mx = fmax(mx, red[q][tid]);
-    int e = 0;
-    if (mx != 0.0) frexp(mx, &e);
+    int e = exps[r0 + tid];
+    if (e == EXP_NONE) e = 0;  // all-zero (or padding) line
     sexp[tid] = e;
-    exps[r0 + tid] = e;
   }
   __syncthreads();
-
-  // ---- phase 2: digits, 32 lines x 64 k per step, 8 consecutive k per thread
+  if (blockIdx.y == 0 && tid < SP_LINES) exps[r0 + tid] = sexp[tid];
   const size_t plane = (size_t)rows_pad * (size_t)k_pad;
-  for (int64_t l0 = 0; l0 < k_pad; l0 += SP_L) {
+  const int64_t kbeg = (int64_t)blockIdx.y * SP_KCHUNK;
+  const int64_t kend = kbeg + SP_KCHUNK < k_pad ? kbeg + SP_KCHUNK : k_pad;
+  for (int64_t l0 = kbeg; l0 < kend; l0 += SP_L) {
     if (TRANS == 0) {
       const int r = tid & 31, cg = tid >> 5;
       for (int c = cg; c < SP_L; c += 8) {
-        int64_t l = l0 + c;
+        const int64_t l = l0 + c;
         tile[r][c] = (r0 + r < rows && l < kk) ? X[(r0 + r) + l * ld] : 0.0;
       }
     } else {
       const int c = tid & 63, rq = tid >> 6;
       for (int r = rq; r < SP_LINES; r += 4) {
-        int64_t l = l0 + c;
+        const int64_t l = l0 + c;
         tile[r][c] = (r0 + r < rows && l < kk) ? X[l + (r0 + r) * ld] : 0.0;
       }
     }
@@ -135,17 +192,15 @@ oz_split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t 
     {
       const int r = tid >> 3, c8 = (tid & 7) * 8;
       const int e = sexp[r];
-      double t[8];
+      DigitState st[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) t[q] = scalbn(tile[r][c8 + q], -e) * 16.0;
+      for (int q = 0; q < 8; ++q) st[q].init(tile[r][c8 + q], e);
       uint8_t* dst = digits + (size_t)(r0 + r) * (size_t)k_pad + (size_t)(l0 + c8);
       for (int p = 0; p < s; ++p) {
         uint32_t lo = 0, hi = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          double d = rint(t[q]);
-          t[q] = (t[q] - d) * 32.0;
-          uint32_t b = digit_byte((int)d, enc);
+          const uint32_t b = digit_byte(st[q].next(), enc);
           if (q < 4) lo |= b << (8 * q);
           else hi |= b << (8 * (q - 4));
         }
@@ -323,13 +378,20 @@ size_t ozaki_workspace_bytes(int engine) { return engine == OZ_ENGINE_TCGEN05 ? 
 cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int64_t kk, const OzakiSplit& out,
                         cudaStream_t s) {
   if (out.slices < 1 || out.slices > OZ_MAX_SLICES) return cudaErrorInvalidValue;
-  unsigned blocks = (unsigned)(out.rows_pad / SP_LINES);
+  cudaError_t e = cudaMemsetAsync(out.exps, 0x80, (size_t)out.rows_pad * sizeof(int32_t), s);  // EXP_NONE
+  if (e != cudaSuccess) return e;
+  if (rows > 0 && kk > 0) {
+    dim3 gm((unsigned)((rows + MX_LINES - 1) / MX_LINES), (unsigned)((kk + MX_KCHUNK - 1) / MX_KCHUNK));
+    if (trans == OP_N) oz_linemax_kernel<0><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps);
+    else oz_linemax_kernel<1><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps);
+  }
+  dim3 gd((unsigned)(out.rows_pad / SP_LINES), (unsigned)((out.k_pad + SP_KCHUNK - 1) / SP_KCHUNK));
   if (trans == OP_N)
-    oz_split_kernel<0><<<blocks, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                     out.slices, out.enc);
+    oz_digits_kernel<0><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
+                                                  out.slices, out.enc);
   else
-    oz_split_kernel<1><<<blocks, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                     out.slices, out.enc);
+    oz_digits_kernel<1><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
+                                                  out.slices, out.enc);
   return cudaGetLastError();
 }
 

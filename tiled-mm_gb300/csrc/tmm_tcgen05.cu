@@ -24,6 +24,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "tmm_ozaki.h"
@@ -94,6 +95,25 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -128,6 +148,13 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// arrive on the same-offset mbarrier of every CTA in `mask` when this thread's MMAs complete
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+               "h"(mask)
+               : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -173,6 +200,18 @@ struct Seq {
   }
 };
 
+// Tile order: bands of GROUP_M tile rows, n-tiles fastest inside a band, so the
+// ~150 co-resident CTAs cover about 16 x 9 tiles and share their A and B panels
+// in L2 (an m-fastest order has them cover 64 A panels per wave at 8192^2).
+constexpr int GROUP_M = 16;
+__device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, int group, int* tm, int* tn) {
+  const int per_band = group * tiles_n;
+  const int band = tile / per_band, local = tile - band * per_band;
+  const int rows_in_band = min(group, tiles_m - band * group);
+  *tm = band * group + local % rows_in_band;
+  *tn = local / rows_in_band;
+}
+
 struct Params {
   const int32_t* ea;
   const int32_t* eb;
@@ -188,6 +227,12 @@ struct Params {
   int tiles_m, tiles_n;
 };
 
+// CM CTAs of a cluster compute the tiles (CM*g + r, n) for r = 0..CM-1: they need
+// the same B tile, of which each CTA loads 1/CM and multicasts it to all, so the
+// L2->SM operand traffic per CTA drops from 48 KB to 16 + 32/CM KB per k-block.
+// A stage is refilled only after every CTA's MMAs have read it (the empty
+// barrier counts one commit per CTA, sent by multicast).
+template <int CM>
 __global__ void __launch_bounds__(THREADS, 1)
 oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -199,12 +244,18 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
-  const int total_tiles = P.tiles_m * P.tiles_n;
+  const int rank = CM > 1 ? (int)cluster_ctarank() : 0;
+  const int cluster_id = blockIdx.x / CM, num_clusters = gridDim.x / CM;
+  const int tiles_mg = (P.tiles_m + CM - 1) / CM;  // cluster tile rows (a last partial group computes padding)
+  const int total_ctiles = tiles_mg * P.tiles_n;
+  const int group = GROUP_M / CM > 0 ? GROUP_M / CM : 1;
+  constexpr uint16_t MASK = (uint16_t)((1u << CM) - 1);
+  constexpr int B_SLICE = BN / CM;  // rows of B this CTA loads and multicasts
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
       mbar_init(full0 + 8 * i, 1);
-      mbar_init(empty0 + 8 * i, 1);
+      mbar_init(empty0 + 8 * i, CM);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(tfull0 + 8 * i, 1);
@@ -220,6 +271,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   if (warp == 1) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
   tc_fence_before();
   __syncthreads();
+  if (CM > 1) cluster_sync();  // peers' barriers are initialised before any multicast lands
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
@@ -229,17 +281,22 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
-        const int tm = tile % P.tiles_m, tn = tile / P.tiles_m;
+      for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
+        int tmg, tn;
+        tile_coords(ct, tiles_mg, P.tiles_n, group, &tmg, &tn);
+        const int tm = tmg * CM + rank;
         Seq q;
         for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
           ok = mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
           if (!ok) break;
           const uint32_t fb = full0 + 8 * stage;
-          mbar_expect_tx(fb, STAGE_BYTES);
+          mbar_expect_tx(fb, STAGE_BYTES);  // own A + every CTA's B slice
           uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
           tma_load_2d(smem_u32(sa), &tmA, q.kb * KB, (int)(q.p * P.a_rows_pad + (int64_t)tm * BM), fb);
-          tma_load_2d(smem_u32(sa + A_BYTES), &tmB, q.kb * KB, (int)((q.g - q.p) * P.b_rows_pad + (int64_t)tn * BN), fb);
+          const int by = (int)((q.g - q.p) * P.b_rows_pad + (int64_t)tn * BN + rank * B_SLICE);
+          const uint32_t bdst = smem_u32(sa + A_BYTES + rank * B_SLICE * KB);
+          if (CM > 1) tma_load_2d_mc(bdst, &tmB, q.kb * KB, by, fb, MASK);
+          else tma_load_2d(bdst, &tmB, q.kb * KB, by, fb);
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
@@ -263,7 +320,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       uint32_t tphase[2] = {0, 0};
       int buf = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+      for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
         Seq q;
         for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
           const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
@@ -280,7 +337,9 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 #pragma unroll
           for (int kk = 0; kk < KB / 32; ++kk)  // K = 32 e4m3 = 32 bytes per MMA: +2 in the 16-byte address field
             mma_f8(d_tmem, ad + 2 * kk, bd + 2 * kk, (q.pass_first() && kk == 0) ? 0u : 1u);
-          mma_commit(empty0 + 8 * stage);  // the stage is free when these MMAs have read it
+          // the stage is free (in every CTA of the cluster) when these MMAs have read it
+          if (CM > 1) mma_commit_mc(empty0 + 8 * stage, MASK);
+          else mma_commit(empty0 + 8 * stage);
           if (q.pass_last()) {
             mma_commit(tfull0 + 8 * buf);
             tphase[buf] ^= 1;
@@ -306,8 +365,10 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     uint32_t tphase[2] = {0, 0};
     int buf = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
-      const int tm = tile % P.tiles_m, tn = tile / P.tiles_m;
+    for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
+      int tmg, tn;
+      tile_coords(ct, tiles_mg, P.tiles_n, group, &tmg, &tn);
+      const int tm = tmg * CM + rank;
       bool first_pass = true;
       Seq q;
       for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
@@ -360,7 +421,9 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     }
   }
   tc_fence_before();
+  __syncwarp();  // lane 0 of warps 0 and 1 ran alone: the cluster barrier below is warp-collective
   __syncthreads();
+  if (CM > 1) cluster_sync();  // no peer multicasts into this CTA after it leaves
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
@@ -406,6 +469,58 @@ int num_sms() {
   return sms;
 }
 
+// Persistent launch: as many clusters as can be resident at once (a cluster's
+// CTAs must share a GPC), capped by the number of cluster tiles.
+template <int CM>
+cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
+  static std::once_flag once;
+  static cudaError_t setup = cudaSuccess;
+  static int max_clusters = 0;
+  std::call_once(once, [] {
+    setup = cudaFuncSetAttribute(oz_gemm_tc<CM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (setup != cudaSuccess) return;
+    if (CM == 1) {
+      max_clusters = num_sms();
+      return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CM;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)((num_sms() / CM) * CM));
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    setup = cudaOccupancyMaxActiveClusters(&max_clusters, oz_gemm_tc<CM>, &cfg);
+    if (setup == cudaSuccess && max_clusters <= 0) setup = cudaErrorInvalidConfiguration;
+  });
+  if (setup != cudaSuccess) return setup;
+  const int tiles_mg = (P.tiles_m + CM - 1) / CM;
+  const int ctiles = tiles_mg * P.tiles_n;
+  const int clusters = ctiles < max_clusters ? ctiles : max_clusters;
+  if ((size_t)clusters * CM > (size_t)num_sms()) return cudaErrorInvalidConfiguration;  // workspace has one slot per SM
+  if (CM == 1) {
+    oz_gemm_tc<1><<<clusters, THREADS, SMEM_BYTES, s>>>(ma, mb, P);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CM;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(clusters * CM));
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = SMEM_BYTES;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, oz_gemm_tc<CM>, ma, mb, P);
+}
+
 }  // namespace tc
 
 size_t ozaki_tc_workspace_bytes() { return (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
@@ -420,16 +535,7 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
     return cudaErrorInvalidValue;
   // TMA coordinates are 32-bit: the stacked planes must stay addressable
   if ((int64_t)A.slices * A.rows_pad > INT32_MAX || (int64_t)B.slices * B.rows_pad > INT32_MAX) return cudaErrorInvalidValue;
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(tc::oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES);
-  });
-  if (attr != cudaSuccess) return attr;
   CUtensorMap ma, mb;
-  cudaError_t e = tc::make_map(&ma, A, tc::BM);
-  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN);
-  if (e != cudaSuccess) return e;
   tc::Params P;
   P.ea = A.exps;
   P.eb = B.exps;
@@ -448,10 +554,22 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.err = err;
   P.tiles_m = (int)((m + tc::BM - 1) / tc::BM);
   P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
-  int tiles = P.tiles_m * P.tiles_n;
-  int grid = tiles < tc::num_sms() ? tiles : tc::num_sms();
-  tc::oz_gemm_tc<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, P);
-  return cudaGetLastError();
+  // cluster size: CTAs sharing one B tile (TMM_TC_CLUSTER=1|2|4 overrides)
+  // measured at 8192^3, 13 slices: 1 -> 30.2, 2 -> 30.4, 4 -> 28.3 TFLOP/s (a cluster of 4
+  // leaves SMs idle where a GPC's TPC count is not a multiple of 2)
+  int cm = P.tiles_m >= 2 ? 2 : 1;
+  if (const char* env = getenv("TMM_TC_CLUSTER")) {
+    const int v = atoi(env);
+    if (v == 1 || v == 2 || v == 4) cm = v;
+  }
+  cudaError_t e = tc::make_map(&ma, A, tc::BM);
+  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN / cm);
+  if (e != cudaSuccess) return e;
+  switch (cm) {
+    case 4: return tc::launch<4>(ma, mb, P, s);
+    case 2: return tc::launch<2>(ma, mb, P, s);
+    default: return tc::launch<1>(ma, mb, P, s);
+  }
 }
 
 }  // namespace tmm
