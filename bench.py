@@ -45,6 +45,10 @@ WORKLOADS = {
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
+    "batched512": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
+                       path="batched", tiles=(4096, 4096, 4096), streams=2,
+                       desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
+                            "uniform[-1,1), pinned host buffers, one persistent launch in a captured CUDA graph"),
     "native4096": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=1.0, kind=0, param=0.0,
                        path="native", tiles=(2048, 2048, 2048), streams=2,
                        desc="FP64 GEMM m=n=k=4096 NN, uniform[-1,1), alpha=beta=1, tiles 2048, 2 streams"),
@@ -339,6 +343,72 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     return result
 
 
+def run_batched(args, rank, world, dist, log) -> dict:
+    """512 GEMMs, m, n, k log-uniform in [64, 4096], half FP64 / half FP32, random trans flags,
+    uniform[-1,1) entries, page-locked host buffers: one persistent launch per call, captured
+    (with its copies) into a CUDA graph on the first call and replayed; against a loop of the
+    plain per-problem path on the same problems."""
+    import tiledmm as tmm
+
+    rng = np.random.default_rng(1234 + rank)
+    count = args.batch_count
+    keep, probs = [], []
+    flops = 0.0
+    for i in range(count):
+        dt = np.float64 if i % 2 == 0 else np.float32
+        if args.batch_dtypes != "mixed":
+            dt = np.float64 if args.batch_dtypes == "f64" else np.float32
+        m, n, k = (int(round(np.exp(rng.uniform(np.log(64), np.log(4096))))) for _ in range(3))
+        ta, tb = rng.choice(["N", "T"]), rng.choice(["N", "T"])
+        ar, ac = (m, k) if ta == "N" else (k, m)
+        br, bc = (k, n) if tb == "N" else (n, k)
+        arrs = []
+        for size in (ar * ac, br * bc, m * n):
+            pa = tmm.PinnedArray((size,), dt)
+            pa.array[:] = rng.uniform(-1, 1, size).astype(dt)
+            keep.append(pa)
+            arrs.append(pa.array)
+        probs.append(dict(trans_a=ta, trans_b=tb, m=m, n=n, k=k, alpha=1.0, a=arrs[0], ld_a=ar, b=arrs[1], ld_b=br,
+                          beta=0.0, c=arrs[2], ld_c=m))
+        flops += 2.0 * m * n * k
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    times = []
+    for it in range(args.warmup + args.steps):
+        barrier(dist)
+        t0 = time.perf_counter()
+        tmm.gemm_batched(ctx, probs)
+        t1 = time.perf_counter()
+        if it >= args.warmup:
+            times.append(t1 - t0)
+    st = ctx.stats()
+    t_batch = max_over_ranks(dist, float(np.mean(times)))
+    log(f"batched: {t_batch * 1e3:.1f} ms per call, graph={st['batch_graph']}")
+    # the plain path, one call per problem (contexts per dtype, default tile policy)
+    c64 = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    c32 = tmm.make_context(np.float32, 2, 4096, 4096, 4096)
+    t0 = time.perf_counter()
+    for p in probs:
+        ctxp = c64 if p["a"].dtype == np.float64 else c32
+        tmm.gemm(ctxp, p["trans_a"], p["trans_b"], p["m"], p["n"], p["k"], p["alpha"], p["a"], p["ld_a"], p["b"],
+                 p["ld_b"], p["beta"], p["c"], p["ld_c"], pin_host_buffers=False, copy_c_back=True)
+    t_loop = max_over_ranks(dist, time.perf_counter() - t0)
+    log(f"loop of the plain path: {t_loop * 1e3:.1f} ms")
+    f64_flops = sum(2.0 * p["m"] * p["n"] * p["k"] for p in probs if p["a"].dtype == np.float64)
+    for pa in keep:
+        pa.free()
+    return {"value": world * flops / t_batch / 1e12, "ms_per_step": t_batch * 1e3, "gpu_launches": st["kernels"],
+            "e2e": {"value": world * flops / t_batch / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
+                    "d2h_bytes_per_step": st["d2h_bytes"], "note": "the batched call is host-to-host"},
+            "loop_of_plain_path": {"tflops": world * flops / t_loop / 1e12, "seconds": t_loop,
+                                   "speedup_of_batched": t_loop / t_batch},
+            "batch": {"problems": count, "flops": flops, "fp64_flops": f64_flops, "graph": st["batch_graph"]},
+            "roofline": {"bound": "tensor", "achieved": f64_flops / t_batch / 1e12,
+                         "peak": MEASURED_ENGINE_PEAKS["dmma_f64_tflops"], "unit": "TFLOP/s",
+                         "frac": f64_flops / t_batch / 1e12 / MEASURED_ENGINE_PEAKS["dmma_f64_tflops"],
+                         "traffic": None, "kernel": "grouped_kernel (FP64 DMMA items dominate)",
+                         "peak_source": "measured DMMA issue rate on this pool's GB300"}}
+
+
 def cpu_baseline(w, seconds_budget: float = 20.0) -> dict:
     """The reference algorithm's CPU restatement (the oracle: tiled GEMM with the reference's tile
     semantics, per-tile plain GEMM) on a k-slab of the workload, all host threads."""
@@ -377,6 +447,8 @@ def main() -> None:
     ap.add_argument("--workload", default="ozaki32768", choices=sorted(WORKLOADS))
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--engine", default="tcgen05", choices=["tcgen05", "imma"])
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--batch-dtypes", default="mixed", choices=["mixed", "f64", "f32"])
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--skip-native", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
@@ -406,6 +478,17 @@ def main() -> None:
         print(json.dumps(line), flush=True)
         return
 
+    if w["path"] == "batched":
+        res = run_batched(args, rank, world, dist, log)
+        if rank == 0:
+            line = dict(base)
+            line["metric"] = "TFLOP/s of 512 uneven FP64/FP32 GEMMs (one persistent launch, graph replay)"
+            line["dtype"] = "f64+f32"
+            line.update(res)
+            print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     res = run_ours(args, w, rank, world, dist, log)
     if rank == 0:
         line = dict(base)

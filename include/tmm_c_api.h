@@ -128,6 +128,31 @@ int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t m, int64_t
                                   double beta, double* c_dev, int64_t ld_c, int slices, int64_t k_tile,
                                   void* stream);
 
+/* One problem of a batch (tmm_gemm_batched). */
+typedef struct tmm_batch_problem {
+  int dtype;             /* TMM_FLOAT or TMM_DOUBLE */
+  char trans_a, trans_b; /* 'N', 'T' or 'C' */
+  int64_t m, n, k;
+  double alpha, beta;    /* rounded to float for TMM_FLOAT problems */
+  const void* a;
+  int64_t ld_a;
+  const void* b;
+  int64_t ld_b;
+  void* c;
+  int64_t ld_c;
+} tmm_batch_problem;
+
+/* New, no reference counterpart (its users call gpu::gemm once per problem,
+ * src/Tiled-MM/tiled_mm.cpp:492-624): `count` GEMMs of any shapes, FP64 and
+ * FP32 mixed, in one persistent kernel launch over a work list of (problem,
+ * C tile) items, tile shapes per size class from the autotuner.  Operands are
+ * host pointers (device_operands == 0: copied in, results copied back; when
+ * every host buffer is page-locked the copies and the launch are captured
+ * once into a CUDA graph keyed by the batch layout and replayed by later calls
+ * with the same layout) or device pointers (device_operands != 0).
+ * Synchronous; semantics per problem as tmm_gemm with copy_c_back. */
+int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_problem* problems, int device_operands);
+
 /* Replaces mm_handle::get_full_device_buffer_c() (src/Tiled-MM/mm_handle.cpp:162-165)
  * and its device_vector::data()/size()/capacity() (src/Tiled-MM/device_vector.hpp:67-80):
  * the device pointer of the compact (ld = m) result left by copy_c_back == 0. */
@@ -190,6 +215,7 @@ typedef struct tmm_stats {
   int tile_m, tile_n, tile_k, n_streams;
   int path, ozaki_slices;
   double seconds;         /* host wall time of the last call */
+  int batch_graph;        /* last tmm_gemm_batched: 0 no graph, 1 captured, 2 replayed */
 } tmm_stats;
 
 int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);

@@ -230,3 +230,32 @@ def test_device_generator_matches_host(tmm):
         tmm.fill_device(d.data_ptr(), rows, cols, ld, kind, param, seed=5, mat_id=1)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(d.cpu().numpy(), h)
+
+
+@pytest.mark.parametrize("ozaki", [False, True])
+def test_autotune_tile_policy(tmm, ozaki):
+    """The autotuned tile policy picks memory-fitting tiles; results equal the reference policy's on
+    integer inputs (exact for any tiling) and under a small memory cap (out of core)."""
+    rng = np.random.default_rng(31)
+    m, n, k = 1500, 1300, 2100
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k, kind="int09")
+    ref = tmm.make_context(np.float64, 2, 512, 512, 512)
+    auto = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    auto.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
+    capped = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    capped.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
+    capped.set_memory_limit(48 * 1024 * 1024)  # below the ~156 MB the full-size tiles need
+    if ozaki:
+        for x in (ref, auto, capped):
+            x.set_path(tmm.PATH_OZAKI, 2)
+    outs = []
+    for ctx in (ref, auto, capped):
+        cc = c.copy()
+        tmm.gemm(ctx, "T", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, cc, ldc)
+        outs.append(cc)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    tm, tn, tk = auto.get_tile_sizes()
+    assert (tm, tn) == (m, n) and tk <= k  # everything fits: one C tile
+    ctm, ctn, ctk = capped.get_tile_sizes()
+    assert ctm * ctn * ctk < tm * tn * tk  # the cap forces smaller tiles

@@ -84,6 +84,14 @@ struct tmm_context {
   tmm::GrowBuffer pool_a, pool_b, pool_c, full_c, staging, scratch;
   tmm::GrowBuffer oz_work;  // [256-byte error word block][per-stream FP64 workspaces of the tcgen05 engine]
   int oz_engine = 0;
+
+  // batched path: packed operands, device problem records + work list, and the
+  // CUDA graph captured for the last batch layout
+  tmm::GrowBuffer batch_arena, batch_meta;
+  std::vector<unsigned char> batch_key;
+  cudaGraphExec_t batch_exec = nullptr;
+  cudaStream_t batch_aux = nullptr;  // second stream: FP32 items beside the FP64 items
+  cudaEvent_t batch_fork = nullptr, batch_join = nullptr;
   tmm::TileCache cache_a, cache_b;
   std::vector<tmm::CSlot> cslots;  // 2 per stream
   std::vector<cudaEvent_t> staging_free;

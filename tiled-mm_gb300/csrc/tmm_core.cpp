@@ -28,6 +28,7 @@
 #include "tmm_kernels.h"
 #include "tmm_ozaki.h"
 #include "tmm_datagen.h"
+#include "tmm_batched.h"
 
 using tmm::Op;
 
@@ -272,6 +273,12 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   ctx->staging.release();
   ctx->scratch.release();
   ctx->oz_work.release();
+  if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+  if (ctx->batch_aux) cudaStreamDestroy(ctx->batch_aux);
+  if (ctx->batch_fork) cudaEventDestroy(ctx->batch_fork);
+  if (ctx->batch_join) cudaEventDestroy(ctx->batch_join);
+  ctx->batch_arena.release();
+  ctx->batch_meta.release();
   for (auto s : ctx->streams) cudaStreamDestroy(s);
   if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
   if (ctx->prep) cudaStreamDestroy(ctx->prep);
@@ -758,6 +765,21 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
     tm = optimal_tile_size(m, ctx->cur_tile_m, ctx->max_tile_m);
     tn = optimal_tile_size(n, ctx->cur_tile_n, ctx->max_tile_n);
     tk = optimal_tile_size(std::max<int64_t>(k, 1), ctx->cur_tile_k, ctx->max_tile_k);
+  } else if (ctx->tile_policy == TMM_TILE_POLICY_AUTOTUNE) {
+    size_t freeb = 0, total = 0;
+    if (cudaMemGetInfo(&freeb, &total) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "cudaMemGetInfo");
+    size_t budget = freeb + ctx->pool_a.capacity + ctx->pool_b.capacity + ctx->pool_c.capacity + ctx->staging.capacity;
+    if (ctx->memory_limit) budget = std::min(budget, ctx->memory_limit);
+    const tmm::TileChoice tc = tmm::autotune_tiles(ctx->dtype, ozaki, ctx->ozaki_slices > 0 ? ctx->ozaki_slices
+                                                   : tmm::OZ_DEFAULT_SLICES, m, n, std::max<int64_t>(k, 1), budget,
+                                                   ctx->max_tile_m, ctx->max_tile_n, ctx->max_tile_k);
+    tm = tc.tm;
+    tn = tc.tn;
+    tk = tc.tk;
+    if (tc.streams > ctx->n_streams) {
+      int st0 = tmm_set_num_streams(ctx, tc.streams);
+      if (st0) return st0;
+    }
   } else {
     tm = (int)std::min<int64_t>(m, ctx->max_tile_m);
     tn = (int)std::min<int64_t>(n, ctx->max_tile_n);
@@ -976,4 +998,208 @@ extern "C" int tmm_error_metric_f64(char trans_a, char trans_b, int64_t m, int64
   for (double v : worst) w = std::max(w, v);
   *metric = w;
   return TMM_SUCCESS;
+}
+
+// ------------------------------------------------------------------ batched path
+namespace {
+
+bool page_locked(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeHost;
+}
+
+void drop_batch_graph(tmm_context* ctx) {
+  if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+  ctx->batch_exec = nullptr;
+  ctx->batch_key.clear();
+}
+
+// copies in, the persistent launch, copies out (host operands)
+int enqueue_batch(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const tmm_batch_problem* host,
+                  int count, int n_work, int n_f64, int any_k0, cudaStream_t s) {
+  const size_t rec = tmm::batch_problem_record_bytes();
+  const void* dprobs = ctx->batch_meta.ptr;
+  const void* dwork = (const char*)ctx->batch_meta.ptr + (rec * (size_t)count + 255) / 256 * 256;
+  for (int i = 0; i < count; ++i) {
+    const tmm_batch_problem& h = host[i];
+    const tmm::BatchProblem& d = dev[i];
+    const size_t es = h.dtype == TMM_DOUBLE ? 8 : 4;
+    if (d.m == 0 || d.n == 0) continue;
+    if (d.k > 0) {
+      const int64_t ar = d.opa == tmm::OP_N ? d.m : d.k, ac = d.opa == tmm::OP_N ? d.k : d.m;
+      const int64_t br = d.opb == tmm::OP_N ? d.k : d.n, bc = d.opb == tmm::OP_N ? d.n : d.k;
+      TMM_CUDA(ctx, cudaMemcpy2DAsync((void*)d.a, (size_t)ar * es, h.a, (size_t)h.ld_a * es, (size_t)ar * es, (size_t)ac,
+                                      cudaMemcpyHostToDevice, s));
+      TMM_CUDA(ctx, cudaMemcpy2DAsync((void*)d.b, (size_t)br * es, h.b, (size_t)h.ld_b * es, (size_t)br * es, (size_t)bc,
+                                      cudaMemcpyHostToDevice, s));
+      ctx->stats.h2d_bytes += (uint64_t)(ar * ac + br * bc) * es;
+    }
+    if (h.beta != 0.0) {
+      TMM_CUDA(ctx, cudaMemcpy2DAsync(d.c, (size_t)d.m * es, h.c, (size_t)h.ld_c * es, (size_t)d.m * es, (size_t)d.n,
+                                      cudaMemcpyHostToDevice, s));
+      ctx->stats.h2d_bytes += (uint64_t)(d.m * d.n) * es;
+    }
+  }
+  cudaError_t e = tmm::batch_launch(dprobs, count, dwork, n_f64, n_work - n_f64, any_k0, s, ctx->batch_aux,
+                                    ctx->batch_fork, ctx->batch_join);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
+  ctx->stats.kernels += (n_f64 > 0) + (n_work - n_f64 > 0) + (any_k0 ? 1 : 0);
+  for (int i = 0; i < count; ++i) {
+    const tmm_batch_problem& h = host[i];
+    const tmm::BatchProblem& d = dev[i];
+    const size_t es = h.dtype == TMM_DOUBLE ? 8 : 4;
+    if (d.m == 0 || d.n == 0) continue;
+    TMM_CUDA(ctx, cudaMemcpy2DAsync(h.c, (size_t)h.ld_c * es, d.c, (size_t)d.m * es, (size_t)d.m * es, (size_t)d.n,
+                                    cudaMemcpyDeviceToHost, s));
+    ctx->stats.d2h_bytes += (uint64_t)(d.m * d.n) * es;
+  }
+  return TMM_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_problem* probs, int device_operands) {
+  if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: null context");
+  auto t0 = std::chrono::steady_clock::now();
+  ctx->stats = tmm_stats{};
+  if (count < 0 || (count > 0 && !probs)) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: bad count");
+  if (count == 0) return TMM_SUCCESS;
+  DeviceGuard dg(ctx->device);
+  std::vector<tmm::BatchProblem> dev((size_t)count);
+  size_t arena = 0;
+  int any_k0 = 0;
+  for (int i = 0; i < count; ++i) {
+    const tmm_batch_problem& h = probs[i];
+    tmm::BatchProblem& d = dev[i];
+    if (h.dtype != TMM_FLOAT && h.dtype != TMM_DOUBLE)
+      return fail(ctx, TMM_ERROR_NOT_SUPPORTED, "tmm_gemm_batched: problems must be TMM_FLOAT or TMM_DOUBLE");
+    if (!parse_op(h.trans_a, h.dtype, &d.opa) || !parse_op(h.trans_b, h.dtype, &d.opb))
+      return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: trans must be one of N, T, C");
+    if (h.m < 0 || h.n < 0 || h.k < 0) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: negative size");
+    const int64_t ar = d.opa == tmm::OP_N ? h.m : h.k, br = d.opb == tmm::OP_N ? h.k : h.n;
+    if (h.ld_a < std::max<int64_t>(1, ar) || h.ld_b < std::max<int64_t>(1, br) || h.ld_c < std::max<int64_t>(1, h.m))
+      return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: leading dimension too small");
+    if (h.m > 0 && h.n > 0 && (!h.c || (h.k > 0 && (!h.a || !h.b))))
+      return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: null matrix pointer");
+    d.dtype = h.dtype;
+    d.m = h.m;
+    d.n = h.n;
+    d.k = h.k;
+    d.alpha = h.alpha;
+    d.beta = h.beta;
+    d.variant = (h.m > 0 && h.n > 0 && h.k > 0) ? tmm::autotune_batch_variant(h.dtype, h.m, h.n, h.k) : 0;
+    if (h.k == 0 && h.m > 0 && h.n > 0) any_k0 = 1;
+    if (device_operands) {
+      d.a = h.a;
+      d.b = h.b;
+      d.c = h.c;
+      d.lda = h.ld_a;
+      d.ldb = h.ld_b;
+      d.ldc = h.ld_c;
+    } else {  // packed, compact leading dimensions in the arena (offsets filled below)
+      const size_t es = h.dtype == TMM_DOUBLE ? 8 : 4;
+      d.lda = std::max<int64_t>(1, ar);
+      d.ldb = std::max<int64_t>(1, br);
+      d.ldc = std::max<int64_t>(1, h.m);
+      arena += ((size_t)(h.m * h.k) * es + 255) / 256 * 256;
+      arena += ((size_t)(h.k * h.n) * es + 255) / 256 * 256;
+      arena += ((size_t)(h.m * h.n) * es + 255) / 256 * 256;
+    }
+  }
+  cudaStream_t s = ctx->streams[0];
+  if (!device_operands) {
+    void* before = ctx->batch_arena.ptr;
+    TMM_CUDA(ctx, ctx->batch_arena.reserve(arena ? arena : 256));
+    if (ctx->batch_arena.ptr != before) drop_batch_graph(ctx);
+    char* p = (char*)ctx->batch_arena.ptr;
+    for (int i = 0; i < count; ++i) {
+      tmm::BatchProblem& d = dev[i];
+      const size_t es = d.dtype == TMM_DOUBLE ? 8 : 4;
+      d.a = p;
+      p += ((size_t)(d.m * d.k) * es + 255) / 256 * 256;
+      d.b = p;
+      p += ((size_t)(d.k * d.n) * es + 255) / 256 * 256;
+      d.c = p;
+      p += ((size_t)(d.m * d.n) * es + 255) / 256 * 256;
+    }
+  }
+  std::vector<unsigned char> pb, wb;
+  int n_work = 0, n_f64 = 0;
+  tmm::batch_plan(dev, pb, wb, &n_work, &n_f64);
+  if (!ctx->batch_aux) {
+    TMM_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->batch_aux, cudaStreamNonBlocking));
+    TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_fork, cudaEventDisableTiming));
+    TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_join, cudaEventDisableTiming));
+  }
+  const int kernels = (n_f64 > 0) + (n_work - n_f64 > 0) + any_k0;
+  const size_t pb_al = (pb.size() + 255) / 256 * 256;
+  {
+    void* before = ctx->batch_meta.ptr;
+    TMM_CUDA(ctx, ctx->batch_meta.reserve(pb_al + wb.size() + 256));
+    if (ctx->batch_meta.ptr != before) drop_batch_graph(ctx);
+  }
+  // the layout key: every field of every problem, plus the chosen variants
+  std::vector<unsigned char> key((const unsigned char*)probs, (const unsigned char*)probs + sizeof(tmm_batch_problem) * count);
+  for (auto& d : dev) key.push_back((unsigned char)d.variant);
+  int st = TMM_SUCCESS;
+  if (!device_operands && ctx->batch_exec && key == ctx->batch_key) {
+    TMM_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+    ctx->stats.batch_graph = 2;
+    ctx->stats.kernels = kernels;
+    for (int i = 0; i < count; ++i) {  // same traffic as the captured copies
+      const size_t es = dev[i].dtype == TMM_DOUBLE ? 8 : 4;
+      if (dev[i].m == 0 || dev[i].n == 0) continue;
+      if (dev[i].k > 0) ctx->stats.h2d_bytes += (uint64_t)(dev[i].m * dev[i].k + dev[i].k * dev[i].n) * es;
+      if (probs[i].beta != 0.0) ctx->stats.h2d_bytes += (uint64_t)(dev[i].m * dev[i].n) * es;
+      ctx->stats.d2h_bytes += (uint64_t)(dev[i].m * dev[i].n) * es;
+    }
+  } else {
+    TMM_CUDA(ctx, cudaMemcpy(ctx->batch_meta.ptr, pb.data(), pb.size(), cudaMemcpyHostToDevice));
+    if (!wb.empty())
+      TMM_CUDA(ctx, cudaMemcpy((char*)ctx->batch_meta.ptr + pb_al, wb.data(), wb.size(), cudaMemcpyHostToDevice));
+    if (device_operands) {
+      cudaError_t e = tmm::batch_launch(ctx->batch_meta.ptr, count, (char*)ctx->batch_meta.ptr + pb_al, n_f64,
+                                        n_work - n_f64, any_k0, s, ctx->batch_aux, ctx->batch_fork, ctx->batch_join);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
+      ctx->stats.kernels = kernels;
+    } else {
+      bool pinned = true;
+      for (int i = 0; i < count && pinned; ++i) {
+        const tmm_batch_problem& h = probs[i];
+        if (h.m == 0 || h.n == 0) continue;
+        pinned = page_locked(h.c) && (h.k == 0 || (page_locked(h.a) && page_locked(h.b)));
+      }
+      if (pinned) {
+        drop_batch_graph(ctx);
+        TMM_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, s);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (st) {
+          if (graph) cudaGraphDestroy(graph);
+          return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+          ctx->batch_exec = nullptr;
+          return cuda_fail(ctx, e, "cudaGraphInstantiate");
+        }
+        ctx->batch_key = key;
+        TMM_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+        ctx->stats.batch_graph = 1;
+      } else {
+        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, s);
+        if (st) return st;
+      }
+    }
+  }
+  TMM_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return st;
 }

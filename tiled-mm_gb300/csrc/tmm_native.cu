@@ -11,6 +11,7 @@
 // full FP32/FP64 accuracy, matching cuBLAS's default non-TF32 semantics).
 #include "tmm_datagen.h"
 #include "tmm_kernels.h"
+#include "tmm_sgemm_tile.cuh"
 
 namespace tmm {
 namespace {
@@ -271,6 +272,14 @@ gemm_simt(int opa, int opb, int64_t m, int64_t n, int64_t k, T alpha, const T* _
     }
 }
 
+__global__ void __launch_bounds__(sg::THREADS)
+gemm_f32_sg(int opa, int opb, int64_t m, int64_t n, int64_t k, float alpha, const float* __restrict__ A, int64_t lda,
+            const float* __restrict__ B, int64_t ldb, float beta, float* __restrict__ C, int64_t ldc) {
+  __shared__ __align__(16) float smem[sg::SMEM_FLOATS];
+  sg::tile(opa, opb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, (int64_t)blockIdx.x * sg::BM,
+           (int64_t)blockIdx.y * sg::BN, smem);
+}
+
 template <typename T>
 __global__ void scale_kernel(int64_t m, int64_t n, T beta, T* C, int64_t ldc) {
   int64_t total = m * n;
@@ -330,8 +339,12 @@ cudaError_t launch_gemm_f64(Op opa, Op opb, int64_t m, int64_t n, int64_t k, dou
 cudaError_t launch_gemm_f32(Op opa, Op opb, int64_t m, int64_t n, int64_t k, float alpha, const float* A,
                             int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
                             cudaStream_t s) {
-  return launch_simt<float>(opa == OP_C ? OP_T : opa, opb == OP_C ? OP_T : opb, m, n, k, alpha, A, lda, B, ldb,
-                            beta, C, ldc, s);
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  dim3 grid((unsigned)((m + sg::BM - 1) / sg::BM), (unsigned)((n + sg::BN - 1) / sg::BN));
+  if (grid.y > 65535) return cudaErrorInvalidConfiguration;
+  gemm_f32_sg<<<grid, sg::THREADS, 0, s>>>(opa == OP_N ? 0 : 1, opb == OP_N ? 0 : 1, m, n, k, alpha, A, lda, B, ldb,
+                                           beta, C, ldc);
+  return cudaGetLastError();
 }
 cudaError_t launch_gemm_c32(Op opa, Op opb, int64_t m, int64_t n, int64_t k, cplxf alpha, const cplxf* A,
                             int64_t lda, const cplxf* B, int64_t ldb, cplxf beta, cplxf* C, int64_t ldc,

@@ -57,6 +57,7 @@ SIGNATURES = {
     "tmm_gemm_device": (_ci, [_p, C.c_char, C.c_char, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64, _p]),
     "tmm_ozaki_gemm_device_noalloc": (_ci, [C.c_char, C.c_char, _i64, _i64, _i64, C.c_double, _p, _i64, _p, _i64,
                                             C.c_double, _p, _i64, _ci, _i64, _p]),
+    "tmm_gemm_batched": (_ci, [_p, _ci, _p, _ci]),
     "tmm_get_full_c": (_ci, [_p, C.POINTER(_p), C.POINTER(_sz), C.POINTER(_sz)]),
     "tmm_set_num_streams": (_ci, [_p, _ci]),
     "tmm_get_num_streams": (_ci, [_p, C.POINTER(_ci)]),
@@ -98,7 +99,8 @@ for _name, (_res, _args) in SIGNATURES.items():
 class Stats(C.Structure):
     _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernels", C.c_uint64),
                 ("tiles_loaded", C.c_uint64), ("tiles_reused", C.c_uint64), ("tile_m", _ci), ("tile_n", _ci),
-                ("tile_k", _ci), ("n_streams", _ci), ("path", _ci), ("ozaki_slices", _ci), ("seconds", C.c_double)]
+                ("tile_k", _ci), ("n_streams", _ci), ("path", _ci), ("ozaki_slices", _ci), ("seconds", C.c_double),
+                ("batch_graph", _ci)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -286,6 +288,26 @@ def gemm_device(ctx: MMHandle, trans_a: str, trans_b: str, m: int, n: int, k: in
     st = _lib.tmm_gemm_device(ctx._h, trans_a.encode()[:1], trans_b.encode()[:1], m, n, k, al.ctypes.data, _ptr(a_dev),
                               ld_a, _ptr(b_dev), ld_b, be.ctypes.data, _ptr(c_dev), ld_c, stream)
     _check(st, ctx._h)
+
+
+class BatchProblem(C.Structure):
+    """tmm_batch_problem (include/tmm_c_api.h)."""
+    _fields_ = [("dtype", _ci), ("trans_a", C.c_char), ("trans_b", C.c_char), ("m", _i64), ("n", _i64), ("k", _i64),
+                ("alpha", C.c_double), ("beta", C.c_double), ("a", _p), ("ld_a", _i64), ("b", _p), ("ld_b", _i64),
+                ("c", _p), ("ld_c", _i64)]
+
+
+def gemm_batched(ctx: MMHandle, problems: list[dict], device_operands: bool = False) -> None:
+    """Many GEMMs (FP64 and FP32 mixed) in one persistent launch; each dict has the keys
+    trans_a, trans_b, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c (arrays of float32 or
+    float64, host or, with device_operands, device)."""
+    arr = (BatchProblem * max(1, len(problems)))()
+    for i, p in enumerate(problems):
+        dt = p["a"].dtype if isinstance(p["a"], np.ndarray) else np.dtype(p.get("dtype", np.float64))
+        arr[i] = BatchProblem(_DTYPES[np.dtype(dt)], p["trans_a"].encode()[:1], p["trans_b"].encode()[:1], p["m"],
+                              p["n"], p["k"], float(p["alpha"]), float(p["beta"]), _ptr(p["a"]), p["ld_a"],
+                              _ptr(p["b"]), p["ld_b"], _ptr(p["c"]), p["ld_c"])
+    _check(_lib.tmm_gemm_batched(ctx._h, len(problems), C.cast(arr, C.c_void_p), int(bool(device_operands))), ctx._h)
 
 
 class PinnedArray:
