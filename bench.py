@@ -45,6 +45,13 @@ WORKLOADS = {
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
+    # BASELINE configs[4] at a size this box holds (host RAM 199 GB): k halved to 65536
+    "ooc_ozaki": dict(m=32768, n=32768, k=65536, ta="N", tb="T", alpha=-1.0, beta=1.0, kind=3, param=10.0,
+                      path="ozaki", tiles=(65536, 65536, 32768), streams=2, policy="autotune", pageable=True,
+                      pin=True, copy_back=False,
+                      desc="Out-of-core Ozaki FP64 GEMM m=n=32768, k=65536, NT, alpha=-1, beta=1, N(0,1) x row "
+                           "factors 2^U[-10,10], pageable host buffers registered per call, copy_c_back=false, "
+                           "autotuned tiles and streams"),
     "batched512": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
                        path="batched", tiles=(4096, 4096, 4096), streams=2,
                        desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
@@ -212,9 +219,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     A = torch.empty(a_rows * a_cols, dtype=torch.float64, device=dev)
     B = torch.empty(b_rows * b_cols, dtype=torch.float64, device=dev)
     Cd = torch.empty(m * n, dtype=torch.float64, device=dev)
+    # (the row-factor kinds scale the rows of the stored A and of the stored B)
     tmm.fill_device(A.data_ptr(), a_rows, a_cols, a_rows, w["kind"], w["param"], seed=rank, mat_id=0, stream=sid)
     tmm.fill_device(B.data_ptr(), b_rows, b_cols, b_rows, w["kind"], w["param"], seed=rank, mat_id=1, stream=sid)
-    tmm.fill_device(Cd.data_ptr(), m, n, m, w["kind"], w["param"], seed=rank, mat_id=2, stream=sid)
+    tmm.fill_device(Cd.data_ptr(), m, n, m, w.get("kind_c", w["kind"]), w["param"], seed=rank, mat_id=2, stream=sid)
     C0 = Cd.clone()
     ctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
     if slices:
@@ -283,23 +291,36 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     torch.cuda.empty_cache()
 
     # ---- end to end through the public host-pointer call
-    pa = tmm.PinnedArray((a_rows * a_cols,))
-    pb = tmm.PinnedArray((b_rows * b_cols,))
-    pc = tmm.PinnedArray((m * n,))
-    pa.array[:] = a_h
-    pb.array[:] = b_h
-    del a_h, b_h, A, B, Cd
+    pageable = w.get("pageable", False)
+    if pageable:  # ordinary (pageable) host memory; registered by the call itself when w["pin"]
+        ha, hb, hc = a_h, b_h, c0_h.copy() if c0_h is not None else np.zeros(m * n)
+        keep = []
+    else:
+        pa = tmm.PinnedArray((a_rows * a_cols,))
+        pb = tmm.PinnedArray((b_rows * b_cols,))
+        pc = tmm.PinnedArray((m * n,))
+        pa.array[:] = a_h
+        pb.array[:] = b_h
+        ha, hb, hc = pa.array, pb.array, pc.array
+        keep = [pa, pb, pc]
+        del a_h, b_h
+    c_init = hc.copy() if w["beta"] != 0 else None
+    del A, B, Cd
     torch.cuda.empty_cache()
     hctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
+    if w.get("policy") == "autotune":
+        hctx.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
     if slices:
         hctx.set_path(tmm.PATH_OZAKI, slices)
         hctx.set_ozaki_engine(w["engine"])
+    copy_back = w.get("copy_back", True)
     e2e_times = []
     for it in range(max(1, args.e2e_warmup) + args.e2e_steps):
-        pc.array[:] = 0.0
+        if c_init is not None:
+            hc[:] = c_init
         t0 = time.perf_counter()
-        tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], pa.array, lda, pb.array, ldb, w["beta"], pc.array, m,
-                 pin_host_buffers=False, copy_c_back=True)
+        tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], hc, m,
+                 pin_host_buffers=w.get("pin", False), copy_c_back=copy_back)
         t1 = time.perf_counter()
         if it >= max(1, args.e2e_warmup):
             e2e_times.append(t1 - t0)
@@ -307,11 +328,14 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
     result["e2e"] = {"value": world * flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
                      "d2h_bytes_per_step": st["d2h_bytes"], "seconds_per_step": t_e2e,
-                     "host_buffers": "pinned (cudaHostAlloc)", "steps": args.e2e_steps}
-    result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"]]
+                     "host_buffers": ("pageable, registered inside each call" if w.get("pin") else "pageable")
+                     if pageable else "pinned (cudaHostAlloc)",
+                     "copy_c_back": copy_back, "steps": args.e2e_steps}
+    result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"], st["n_streams"]]
+    result["e2e_tiles_loaded"] = st["tiles_loaded"]
     hctx.close()
     ctx.close()
-    for p in (pa, pb, pc):
+    for p in keep:
         p.free()
 
     if w["path"] == "ozaki":
