@@ -66,11 +66,13 @@ def test_bit_exact_vs_oracle(tmm, oracle, engine, trans, shape, tiles):
     np.testing.assert_array_equal(out, want)
 
 
-@pytest.mark.parametrize("cluster", ["1", "2", "4"])
+@pytest.mark.parametrize("cluster", ["1", "2", "4", "pair"])
 @pytest.mark.parametrize("shape", [(700, 530, 1100), (1100, 300, 700), (129, 600, 257)])
 def test_tcgen05_cluster_sizes_bit_exact(tmm, oracle, monkeypatch, cluster, shape):
     """CTA clusters that share B tiles by multicast (forced sizes 1, 2, 4; row-tile
-    counts that leave padding tiles in the last cluster) give the oracle's bits."""
+    counts that leave padding tiles in the last cluster) and CTA pairs issuing
+    cta_group::2 MMAs on 256 x 256 tiles (a peer CTA whose rows are all padding at
+    m = 129) give the oracle's bits."""
     monkeypatch.setenv("TMM_TC_CLUSTER", cluster)
     m, n, k = shape
     rng = np.random.default_rng(m * 7 + n)

@@ -55,6 +55,7 @@ OzakiSplit ozaki_split_view(void* base, int64_t rows, int64_t kk, int slices, in
   v.k_pad = oz_round_up(kk > 0 ? kk : 1, OZ_K_ALIGN);
   v.slices = slices;
   v.enc = ozaki_encoding(engine);
+  v.blocked = engine == OZ_ENGINE_TCGEN05 ? 1 : 0;
   size_t digits = (size_t)slices * (size_t)v.rows_pad * (size_t)v.k_pad;
   digits = (digits + 1023) / 1024 * 1024;
   v.digits = (uint8_t*)base;
@@ -159,7 +160,7 @@ struct DigitState {
 template <int TRANS>
 __global__ void __launch_bounds__(SP_THREADS)
 oz_digits_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, uint8_t* __restrict__ digits,
-                 int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc) {
+                 int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc, int blocked) {
   __shared__ double tile[SP_LINES][SP_L + 1];
   __shared__ int sexp[SP_LINES];
   const int tid = threadIdx.x;
@@ -195,7 +196,8 @@ oz_digits_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t
       DigitState st[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) st[q].init(tile[r][c8 + q], e);
-      uint8_t* dst = digits + (size_t)(r0 + r) * (size_t)k_pad + (size_t)(l0 + c8);
+      // 8 consecutive digits of one line never straddle a 128-byte block row
+      uint8_t* dst = digits + oz_digit_offset(r0 + r, l0 + c8, k_pad, blocked);
       for (int p = 0; p < s; ++p) {
         uint32_t lo = 0, hi = 0;
 #pragma unroll
@@ -388,10 +390,10 @@ cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int
   dim3 gd((unsigned)(out.rows_pad / SP_LINES), (unsigned)((out.k_pad + SP_KCHUNK - 1) / SP_KCHUNK));
   if (trans == OP_N)
     oz_digits_kernel<0><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                  out.slices, out.enc);
+                                                  out.slices, out.enc, out.blocked);
   else
     oz_digits_kernel<1><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                  out.slices, out.enc);
+                                                  out.slices, out.enc, out.blocked);
   return cudaGetLastError();
 }
 

@@ -1,8 +1,8 @@
 // Internal interface of the Ozaki split-precision FP64 engine (not part of the C ABI).
 //
 // A double tile op(X) (lines x kk along k) is split into s digit planes of
-// small integers |d| <= 16 stored one byte per digit, K-major
-// [s][rows_pad][k_pad], plus one power-of-two exponent per line; the product
+// small integers |d| <= 16 stored one byte per digit, K-major, plus one
+// power-of-two exponent per line (digit layouts: see OzakiSplit); the product
 // of two split tiles is a sum of exact integer tile GEMMs on the tensor cores,
 // recombined in FP64 with the alpha/beta epilogue fused.  tmm_ozaki.cu holds
 // the algorithm and its published sources.
@@ -25,13 +25,28 @@ enum OzEnc : int { OZ_ENC_INT8 = 0, OZ_ENC_E4M3 = 1 };
 // slice-product engines
 enum OzEngine : int { OZ_ENGINE_IMMA = 0, OZ_ENGINE_TCGEN05 = 1 };
 
+// Digit layouts.  Plain (IMMA engine): [s][rows_pad][k_pad], line-major.
+// Blocked (tcgen05 engine): [s][rows_pad/128][k_pad/128][128 lines][128 bytes]:
+// the 128-line x 128-byte box a tensor-core stage loads is one contiguous 16 KB
+// block of HBM (in the plain layout it is 128 segments of 128 bytes, k_pad apart,
+// nearly every one opening its own DRAM page).
+constexpr int OZ_BLOCK = 128;
+
 struct OzakiSplit {
-  uint8_t* digits = nullptr;  // [s][rows_pad][k_pad]
+  uint8_t* digits = nullptr;  // plain or blocked (above)
   int32_t* exps = nullptr;    // [rows_pad]
   int64_t rows = 0, kk = 0, rows_pad = 0, k_pad = 0;
   int slices = 0;
   int enc = OZ_ENC_INT8;
+  int blocked = 0;
 };
+
+// byte offset of digit (line r, element l) in slice 0 of a split (add p * rows_pad * k_pad for slice p)
+inline __host__ __device__ size_t oz_digit_offset(int64_t r, int64_t l, int64_t k_pad, int blocked) {
+  if (!blocked) return (size_t)r * (size_t)k_pad + (size_t)l;
+  return ((size_t)(r / OZ_BLOCK) * (size_t)(k_pad / OZ_BLOCK) + (size_t)(l / OZ_BLOCK)) * (OZ_BLOCK * OZ_BLOCK) +
+         (size_t)(r % OZ_BLOCK) * OZ_BLOCK + (size_t)(l % OZ_BLOCK);
+}
 
 inline int64_t oz_round_up(int64_t v, int64_t q) { return (v + q - 1) / q * q; }
 

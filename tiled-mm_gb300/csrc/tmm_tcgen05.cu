@@ -20,11 +20,17 @@
 // (oracle/tmm_ozaki_oracle.c) replays.  Every mbarrier wait is bounded: after
 // about a second it records an error word and the CTA winds down (waiting,
 // again bounded, for its copies and MMAs in flight) and frees its TMEM.
+//
+// A second form (oz_gemm_tc_pair, selected with TMM_TC_CLUSTER=pair) runs the
+// same sequence on CTA pairs with tcgen05.mma.cta_group::2 on 256 x 256 tiles.
+// Digit planes are read in the blocked layout (tmm_ozaki.h): every box a stage
+// loads is one contiguous 16 KB block.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "tmm_ozaki.h"
@@ -104,6 +110,12 @@ __device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* 
       : "memory");
 }
 
+// L2 prefetch of the box at (x, y): a hint, nothing waits for it
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)map), "r"(x), "r"(y)
+               : "memory");
+}
+
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -153,6 +165,85 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 // arrive on the same-offset mbarrier of every CTA in `mask` when this thread's MMAs complete
 __device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+               "h"(mask)
+               : "memory");
+}
+
+// ---- CTA-pair (cta_group::2) forms
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t cta) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(cta));
+  return r;
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait of the pair engine.  A timeout raises this CTA's and the peer's
+// abort flags; with honor_abort false (the final drains) only the timeout ends it,
+// so copies and MMAs in flight finish before TMEM is freed.  CLUSTER_ACQ: acquire
+// at cluster scope (a barrier that the peer's threads arrive on); copies and MMA
+// commits signal their barriers through the async proxy and need only the default.
+template <bool CLUSTER_ACQ>
+__device__ __forceinline__ bool mbar_wait_pair(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                               uint32_t peer_abort, int* err, bool honor_abort = true) {
+  auto probe = [&] { return CLUSTER_ACQ ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity); };
+  for (int i = 0; i < 256; ++i)
+    if (probe()) return true;
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    if (probe()) return true;
+    if (honor_abort && *abort_flag) return false;
+    if (globaltimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(peer_abort), "r"(1) : "memory");
+      atomicOr(err, 1);
+      return false;
+    }
+  }
+}
+
+// the leader's and the peer's TMEM allocation is one collective (one warp in each CTA)
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t slot_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_smem), "r"(ncols));
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+// copy into this CTA's shared memory, bytes counted on the (leader's) barrier at a cluster address
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar_cluster)
+      : "memory");
+}
+
+// kind::f8f6f4 across the pair: M = 256 (128 TMEM lanes in each CTA), N = 256
+constexpr uint32_t IDESC_PAIR = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+
+__device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC_PAIR), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
                "h"(mask)
                : "memory");
 }
@@ -212,6 +303,13 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
   *tn = local / rows_in_band;
 }
 
+// Digit planes are in the blocked layout ([s][rows/128][k/128][128][128] bytes); the
+// tensor maps view them as rows of 128 bytes.  Row coordinate of the box that starts
+// at line `line` (a multiple of the box height, which divides 128) of slice p, k-block kb:
+__device__ __forceinline__ int box_y(int p, int64_t line, int kb, int64_t rows_pad, int nkb) {
+  return (int)((((int64_t)p * (rows_pad / OZ_BLOCK) + line / OZ_BLOCK) * nkb + kb) * OZ_BLOCK + line % OZ_BLOCK);
+}
+
 struct Params {
   const int32_t* ea;
   const int32_t* eb;
@@ -225,6 +323,7 @@ struct Params {
   double* work;  // gridDim.x slots of BM * BN doubles
   int* err;
   int tiles_m, tiles_n;
+  int pf;  // k-blocks the producer prefetches into L2 ahead of its loads (0: none)
 };
 
 // CM CTAs of a cluster compute the tiles (CM*g + r, n) for r = 0..CM-1: they need
@@ -251,6 +350,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   const int group = GROUP_M / CM > 0 ? GROUP_M / CM : 1;
   constexpr uint16_t MASK = (uint16_t)((1u << CM) - 1);
   constexpr int B_SLICE = BN / CM;  // rows of B this CTA loads and multicasts
+  constexpr int B_BOX = B_SLICE < OZ_BLOCK ? B_SLICE : OZ_BLOCK;  // a box stays inside one 128-line block
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -285,18 +385,35 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         int tmg, tn;
         tile_coords(ct, tiles_mg, P.tiles_n, group, &tmg, &tn);
         const int tm = tmg * CM + rank;
-        Seq q;
+        // f runs P.pf k-blocks ahead of q: its boxes are prefetched into L2 so that the
+        // loads, issued when a stage frees up, find them there instead of in DRAM
+        const int64_t b0 = (int64_t)tn * BN + rank * B_SLICE;
+        auto prefetch = [&](const Seq& f) {
+          tma_prefetch_2d(&tmA, 0, box_y(f.p, (int64_t)tm * BM, f.kb, P.a_rows_pad, P.nkb));
+          for (int j = 0; j < B_SLICE / B_BOX; ++j)
+            tma_prefetch_2d(&tmB, 0, box_y(f.g - f.p, b0 + j * B_BOX, f.kb, P.b_rows_pad, P.nkb));
+        };
+        Seq q, f;
+        f.start(P.s, P.nkb);
+        for (int i = 0; i < P.pf && !f.done(); ++i, f.next()) prefetch(f);
         for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+          if (P.pf > 0 && !f.done()) {
+            prefetch(f);
+            f.next();
+          }
           ok = mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
           if (!ok) break;
           const uint32_t fb = full0 + 8 * stage;
           mbar_expect_tx(fb, STAGE_BYTES);  // own A + every CTA's B slice
           uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
-          tma_load_2d(smem_u32(sa), &tmA, q.kb * KB, (int)(q.p * P.a_rows_pad + (int64_t)tm * BM), fb);
-          const int by = (int)((q.g - q.p) * P.b_rows_pad + (int64_t)tn * BN + rank * B_SLICE);
-          const uint32_t bdst = smem_u32(sa + A_BYTES + rank * B_SLICE * KB);
-          if (CM > 1) tma_load_2d_mc(bdst, &tmB, q.kb * KB, by, fb, MASK);
-          else tma_load_2d(bdst, &tmB, q.kb * KB, by, fb);
+          tma_load_2d(smem_u32(sa), &tmA, 0, box_y(q.p, (int64_t)tm * BM, q.kb, P.a_rows_pad, P.nkb), fb);
+#pragma unroll
+          for (int j = 0; j < B_SLICE / B_BOX; ++j) {
+            const int by = box_y(q.g - q.p, b0 + j * B_BOX, q.kb, P.b_rows_pad, P.nkb);
+            const uint32_t bdst = smem_u32(sa + A_BYTES + (rank * B_SLICE + j * B_BOX) * KB);
+            if (CM > 1) tma_load_2d_mc(bdst, &tmB, 0, by, fb, MASK);
+            else tma_load_2d(bdst, &tmB, 0, by, fb);
+          }
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
@@ -431,6 +548,223 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   }
 }
 
+// ------------------------------------------------------------------ CTA-pair engine
+// The two CTAs of a cluster pair (on the two SMs of a TPC) compute one 256 x 256
+// tile with tcgen05.mma.cta_group::2 (M = 256, N = 256, K = 32): CTA r stages rows
+// 128 r .. 128 r + 127 of the A tile and of the B tile, so an SM takes in 32 KB per
+// k-block for its 128 x 256 half (48 KB for the same half on one SM), and the MMA
+// reads the B tile from both SMs.  The even CTA (leader) issues all MMAs; both
+// CTAs' copies count their bytes on the leader's full barrier; the leader's commits
+// arrive on both CTAs' empty and accumulator-full barriers; both CTAs' epilogue
+// warps release an accumulator on the leader's empty-accumulator barrier (8
+// arrivals).  Each CTA drains its own 128 TMEM lanes = its 128 tile rows, with the
+// pass sequence, FP64 recombination and fused epilogue of oz_gemm_tc.
+constexpr int PAIR_M = 256;
+constexpr int PAIR_STAGES = 6;
+constexpr int PAIR_A_BYTES = 128 * KB, PAIR_B_BYTES = 128 * KB, PAIR_STAGE_BYTES = PAIR_A_BYTES + PAIR_B_BYTES;
+constexpr size_t PAIR_SMEM_BYTES = (size_t)PAIR_STAGES * PAIR_STAGE_BYTES + 1024 + 256;
+
+__global__ void __launch_bounds__(THREADS, 1)
+oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + (size_t)PAIR_STAGES * PAIR_STAGE_BYTES);
+  // bars: full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2]
+  volatile int* abort_flag = (volatile int*)(bars + 2 * PAIR_STAGES + 4);
+  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * PAIR_STAGES + 5);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_ctarank();  // 0: leader
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + PAIR_STAGES);
+  const uint32_t tfull0 = smem_u32(bars + 2 * PAIR_STAGES), tempty0 = smem_u32(bars + 2 * PAIR_STAGES + 2);
+  const uint32_t lead_full0 = mapa(full0, 0), lead_tempty0 = mapa(tempty0, 0);
+  const uint32_t peer_abort = mapa(smem_u32((const void*)abort_flag), rank ^ 1u);
+  const int pair_id = blockIdx.x >> 1, num_pairs = gridDim.x >> 1;
+  const int total_tiles = P.tiles_m * P.tiles_n;  // tiles_m counts 256-row tiles here
+  constexpr int group = GROUP_M / 2;
+  constexpr uint16_t BOTH = 3;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < PAIR_STAGES; ++i) {
+      mbar_init(full0 + 8 * i, 1);   // the leader's expect_tx arrival (+ both CTAs' bytes)
+      mbar_init(empty0 + 8 * i, 1);  // one multicast commit
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(tfull0 + 8 * i, 1);
+      mbar_init(tempty0 + 8 * i, 8);  // four epilogue warps in each CTA (used in the leader)
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0 && lane == 0) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == 1) tmem_alloc_pair(smem_u32(tmem_slot), TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();  // both CTAs' barriers are initialised before any copy or commit lands
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- TMA producer (both CTAs)
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int ct = pair_id; ct < total_tiles && ok; ct += num_pairs) {
+        int tm, tn;
+        tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
+        const int64_t arow = (int64_t)tm * PAIR_M + rank * 128;
+        const int64_t brow = (int64_t)tn * BN + rank * 128;
+        auto prefetch = [&](const Seq& f) {  // as in oz_gemm_tc
+          tma_prefetch_2d(&tmA, 0, box_y(f.p, arow, f.kb, P.a_rows_pad, P.nkb));
+          tma_prefetch_2d(&tmB, 0, box_y(f.g - f.p, brow, f.kb, P.b_rows_pad, P.nkb));
+        };
+        Seq q, f;
+        f.start(P.s, P.nkb);
+        for (int i = 0; i < P.pf && !f.done(); ++i, f.next()) prefetch(f);
+        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+          if (P.pf > 0 && !f.done()) {
+            prefetch(f);
+            f.next();
+          }
+          ok = mbar_wait_pair<false>(empty0 + 8 * stage, phase ^ 1, abort_flag, peer_abort, P.err);
+          if (!ok) break;
+          if (rank == 0) mbar_expect_tx(full0 + 8 * stage, 2 * PAIR_STAGE_BYTES);
+          uint8_t* sa = smem + (size_t)stage * PAIR_STAGE_BYTES;
+          const uint32_t fb = lead_full0 + 8 * stage;
+          tma_load_2d_pair(smem_u32(sa), &tmA, 0, box_y(q.p, arow, q.kb, P.a_rows_pad, P.nkb), fb);
+          tma_load_2d_pair(smem_u32(sa + PAIR_A_BYTES), &tmB, 0, box_y(q.g - q.p, brow, q.kb, P.b_rows_pad, P.nkb), fb);
+          if (++stage == PAIR_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // drain: every copy issued has been consumed before the CTA may exit (bounded)
+      for (int i = 0; i < PAIR_STAGES; ++i) {
+        (void)mbar_wait_pair<false>(empty0 + 8 * stage, phase ^ 1, abort_flag, peer_abort, P.err, false);
+        if (++stage == PAIR_STAGES) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- MMA issuer (leader)
+    if (lane == 0 && rank == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t tphase[2] = {0, 0};
+      int buf = 0;
+      bool ok = true;
+      for (int ct = pair_id; ct < total_tiles && ok; ct += num_pairs) {
+        Seq q;
+        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+          if (q.pass_first()) {
+            ok = mbar_wait_pair<true>(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, peer_abort, P.err);
+            if (!ok) break;
+            tc_fence_after();
+          }
+          ok = mbar_wait_pair<false>(full0 + 8 * stage, phase, abort_flag, peer_abort, P.err);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + (size_t)stage * PAIR_STAGE_BYTES);
+          const uint64_t ad = smem_desc(sa), bd = smem_desc(sa + PAIR_A_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < KB / 32; ++kk)
+            mma_f8_pair(d_tmem, ad + 2 * kk, bd + 2 * kk, (q.pass_first() && kk == 0) ? 0u : 1u);
+          mma_commit_pair(empty0 + 8 * stage, BOTH);  // the stage is free in both CTAs
+          if (q.pass_last()) {
+            mma_commit_pair(tfull0 + 8 * buf, BOTH);
+            tphase[buf] ^= 1;
+            buf ^= 1;
+          }
+          if (++stage == PAIR_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // both accumulators released by both CTAs: no MMA is in flight when TMEM is freed
+      for (int b = 0; b < 2; ++b) {
+        (void)mbar_wait_pair<true>(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, peer_abort, P.err, false);
+        buf ^= 1;
+      }
+    }
+  } else {
+    // ---------------------------------------------------------------- epilogue (warps 2..5, both CTAs)
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;  // TMEM lane = row of this CTA's half of the tile
+    double* slot = P.work + (size_t)blockIdx.x * (size_t)(BM * BN);
+    uint32_t tphase[2] = {0, 0};
+    int buf = 0;
+    bool ok = true;
+    for (int ct = pair_id; ct < total_tiles && ok; ct += num_pairs) {
+      int tm, tn;
+      tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
+      bool first_pass = true;
+      Seq q;
+      for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+        if (!q.pass_last()) continue;
+        int okw = 1;
+        if (lane == 0) okw = mbar_wait_pair<false>(tfull0 + 8 * buf, tphase[buf], abort_flag, peer_abort, P.err) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
+        __syncwarp();
+        if (!ok) break;
+        tc_fence_after();
+        const double wg = scalbn(1.0, -OZ_DIGIT_BITS * q.g);
+        const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
+#pragma unroll 1
+        for (int c = 0; c < BN / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tbase + (uint32_t)(c * 32), r);
+          tmem_ld_wait();
+          if (c == BN / 32 - 1) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(lead_tempty0 + 8 * buf);
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            double* w = slot + (size_t)(c * 32 + j) * BM + row;
+            const double v = (double)__uint_as_float(r[j]);
+            *w = (first_pass ? 0.0 : *w) + wg * v;
+          }
+        }
+        first_pass = false;
+        tphase[buf] ^= 1;
+        buf ^= 1;
+      }
+      if (!ok) break;
+      const int64_t gi = (int64_t)tm * PAIR_M + rank * 128 + row;
+      if (gi < P.m) {
+        const int ei = P.ea[gi];
+        for (int col = 0; col < BN; ++col) {
+          const int64_t gj = (int64_t)tn * BN + col;
+          if (gj >= P.n) break;
+          const double t = scalbn(slot[(size_t)col * BM + row], ei + P.eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
+          double* cp = P.C + gi + gj * P.ldc;
+          if (!P.first) *cp = fma(P.alpha, t, *cp);
+          else if (P.beta != 0.0) *cp = fma(P.alpha, t, P.beta * *cp);
+          else *cp = P.alpha * t;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncwarp();
+  __syncthreads();
+  cluster_sync();  // the peer's copies, arrivals and the leader's MMAs into this CTA are over
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc_pair(tmem_base, TMEM_COLS);
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -444,11 +778,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+// the blocked digit planes as one column of 128-byte rows; a box is box_rows (<= 128) of them
 cudaError_t make_map(CUtensorMap* map, const OzakiSplit& X, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
-  cuuint64_t dims[2] = {(cuuint64_t)X.k_pad, (cuuint64_t)X.slices * (cuuint64_t)X.rows_pad};
-  cuuint64_t strides[1] = {(cuuint64_t)X.k_pad};
+  cuuint64_t dims[2] = {(cuuint64_t)KB, (cuuint64_t)X.slices * (cuuint64_t)X.rows_pad * (cuuint64_t)(X.k_pad / KB)};
+  cuuint64_t strides[1] = {(cuuint64_t)KB};
   cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)X.digits, dims, strides, box, estr,
@@ -521,6 +856,37 @@ cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P
   return cudaLaunchKernelEx(&cfg, oz_gemm_tc<CM>, ma, mb, P);
 }
 
+// Persistent launch of the pair engine: clusters of 2 CTAs, as many as can be resident.
+cudaError_t launch_pair(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
+  static std::once_flag once;
+  static cudaError_t setup = cudaSuccess;
+  static int max_pairs = 0;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = PAIR_SMEM_BYTES;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  std::call_once(once, [&cfg] {
+    setup = cudaFuncSetAttribute(oz_gemm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAIR_SMEM_BYTES);
+    if (setup != cudaSuccess) return;
+    cfg.gridDim = dim3((unsigned)((num_sms() / 2) * 2));
+    setup = cudaOccupancyMaxActiveClusters(&max_pairs, oz_gemm_tc_pair, &cfg);
+    if (setup == cudaSuccess && max_pairs <= 0) setup = cudaErrorInvalidConfiguration;
+  });
+  if (setup != cudaSuccess) return setup;
+  const int tiles = P.tiles_m * P.tiles_n;
+  const int pairs = tiles < max_pairs ? tiles : max_pairs;
+  if ((size_t)pairs * 2 > (size_t)num_sms()) return cudaErrorInvalidConfiguration;  // workspace has one slot per SM
+  cfg.gridDim = dim3((unsigned)(pairs * 2));
+  cfg.stream = s;
+  return cudaLaunchKernelEx(&cfg, oz_gemm_tc_pair, ma, mb, P);
+}
+
 }  // namespace tc
 
 size_t ozaki_tc_workspace_bytes() { return (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
@@ -531,10 +897,12 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
                           bool first_k_tile, double* C, int64_t ldc, double* work, int* err, cudaStream_t s) {
   if (m <= 0 || n <= 0) return cudaSuccess;
   if (A.enc != OZ_ENC_E4M3 || B.enc != OZ_ENC_E4M3 || A.k_pad != B.k_pad || A.slices != B.slices ||
-      A.rows_pad % tc::BM || B.rows_pad % tc::BN || A.k_pad % tc::KB || !work || !err)
+      A.rows_pad % tc::BM || B.rows_pad % tc::BN || A.k_pad % tc::KB || !A.blocked || !B.blocked || !work || !err)
     return cudaErrorInvalidValue;
-  // TMA coordinates are 32-bit: the stacked planes must stay addressable
-  if ((int64_t)A.slices * A.rows_pad > INT32_MAX || (int64_t)B.slices * B.rows_pad > INT32_MAX) return cudaErrorInvalidValue;
+  // TMA coordinates are 32-bit: every 128-byte row of the stacked planes must stay addressable
+  if ((int64_t)A.slices * A.rows_pad * (A.k_pad / tc::KB) > INT32_MAX ||
+      (int64_t)B.slices * B.rows_pad * (B.k_pad / tc::KB) > INT32_MAX)
+    return cudaErrorInvalidValue;
   CUtensorMap ma, mb;
   tc::Params P;
   P.ea = A.exps;
@@ -552,18 +920,32 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.ldc = ldc;
   P.work = work;
   P.err = err;
-  P.tiles_m = (int)((m + tc::BM - 1) / tc::BM);
   P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
-  // cluster size: CTAs sharing one B tile (TMM_TC_CLUSTER=1|2|4 overrides)
-  // measured at 8192^3, 13 slices: 1 -> 30.2, 2 -> 30.4, 4 -> 28.3 TFLOP/s (a cluster of 4
-  // leaves SMs idle where a GPC's TPC count is not a multiple of 2)
-  int cm = P.tiles_m >= 2 ? 2 : 1;
+  P.pf = 0;  // measured: any distance (4..32) slows the 8192^3 and 8192^2 x 32768 runs by 30-120 %
+  if (const char* env = getenv("TMM_TC_PREFETCH")) P.pf = atoi(env) < 0 ? 0 : (atoi(env) > 64 ? 64 : atoi(env));
+  // Engine form (TMM_TC_CLUSTER overrides): 1, 2, 4 = one-SM MMA on 128 x 256 tiles in
+  // clusters of that many CTAs sharing B by multicast (2 is the default from two row
+  // tiles up); "pair" = CTA-pair MMA on 256 x 256 tiles.  Cycles per k-block and SM,
+  // 11 slices: 8192^3 -> 904 (2), 896 (pair), 893 (1); 16384^3 -> 924 (2), 925 (pair);
+  // 32768^3 -> 966 (2), 1134 (pair).
+  const int64_t tiles128 = (m + tc::BM - 1) / tc::BM;
+  int cm = tiles128 >= 2 ? 2 : 1;  // 0: pair
   if (const char* env = getenv("TMM_TC_CLUSTER")) {
+    if (!strcmp(env, "pair")) cm = 0;
     const int v = atoi(env);
     if (v == 1 || v == 2 || v == 4) cm = v;
   }
+  if (cm == 0) {
+    if (A.rows_pad % tc::PAIR_M) return cudaErrorInvalidValue;
+    P.tiles_m = (int)((m + tc::PAIR_M - 1) / tc::PAIR_M);
+    cudaError_t e = tc::make_map(&ma, A, 128);
+    if (e == cudaSuccess) e = tc::make_map(&mb, B, 128);
+    if (e != cudaSuccess) return e;
+    return tc::launch_pair(ma, mb, P, s);
+  }
+  P.tiles_m = (int)tiles128;
   cudaError_t e = tc::make_map(&ma, A, tc::BM);
-  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN / cm);
+  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN / cm < OZ_BLOCK ? tc::BN / cm : OZ_BLOCK);
   if (e != cudaSuccess) return e;
   switch (cm) {
     case 4: return tc::launch<4>(ma, mb, P, s);
