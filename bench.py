@@ -40,12 +40,13 @@ MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 151.2, "dmma_f64_tflops": 1.054, "dfma_
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
-                       path="ozaki", tiles=(32768, 32768, 32768), streams=2,
-                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20]"),
+                       path="ozaki", tiles=(32768, 32768, 16384), streams=2,
+                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20], k tiles of 16384"),
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
-    # BASELINE configs[4] at a size this box holds (host RAM 199 GB): k halved to 65536
+    # the out-of-core update m = n = 65536, k = 131072 (NT, alpha = -1, beta = 1) with every dimension
+    # halved, so that its host operands fit this host's 199 GB of RAM
     "ooc_ozaki": dict(m=32768, n=32768, k=65536, ta="N", tb="T", alpha=-1.0, beta=1.0, kind=3, param=10.0,
                       path="ozaki", tiles=(65536, 65536, 32768), streams=2, policy="autotune", pageable=True,
                       pin=True, copy_back=False,
@@ -478,8 +479,11 @@ def main() -> None:
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--e2e-warmup", type=int, default=1)
+    ap.add_argument("--tiles", default="", help="tile_m,tile_n,tile_k of the context (overrides the workload's)")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload], engine=args.engine)
+    if args.tiles:
+        w["tiles"] = tuple(int(x) for x in args.tiles.split(","))
     rank, world, local, dist = dist_setup(args.gpus)
     log = (lambda s: print(s, file=sys.stderr, flush=True)) if rank == 0 else (lambda s: None)
     config = {"workload": w["desc"], "m": w["m"], "n": w["n"], "k": w["k"], "trans": w["ta"] + w["tb"],

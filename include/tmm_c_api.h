@@ -23,7 +23,7 @@
  *     (src/Tiled-MM/device_vector.hpp:93-107);
  *   - the tile-size policy of src/Tiled-MM/mm_handle.cpp:89-133 is the
  *     default (TMM_TILE_POLICY_REFERENCE).
- * Deliberate deviations (documented in the design doc):
+ * Deliberate deviations from the reference:
  *   - 64-bit sizes, leading dimensions and offsets (the reference's int
  *     offsets overflow past 2^31 elements);
  *   - invalid arguments are reported (the reference constructs but never

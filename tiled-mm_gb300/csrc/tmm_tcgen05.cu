@@ -266,7 +266,7 @@ __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.
 struct Seq {
   int s, nkb;
   int g, p, kb;
-  int64_t used;
+  int used;  // k-blocks of the current pass before this one (< PASS_BLOCKS)
   __device__ void start(int s_, int nkb_) {
     s = s_;
     nkb = nkb_;
@@ -287,6 +287,26 @@ struct Seq {
         p = 0;
         --g;
       }
+    }
+  }
+};
+
+// Position of the MMA issuer in its (tile, sequence) order: tiles ct, ct + stride, ...
+struct MmaCursor {
+  Seq q;
+  int ct;
+  bool valid;
+  __device__ void start(int ct0, int total, int s, int nkb) {
+    ct = ct0;
+    valid = ct < total;
+    q.start(s, nkb);
+  }
+  __device__ void next(int stride, int total, int s, int nkb) {
+    q.next();
+    if (q.done()) {
+      ct += stride;
+      valid = ct < total;
+      if (valid) q.start(s, nkb);
     }
   }
 };
@@ -431,46 +451,72 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
+    // The tensor pipe keeps almost no queue of issued MMAs: every cycle this thread spends
+    // between two MMAs is a cycle the pipe idles (a k-block of 4 MMAs takes 512 cycles when
+    // they are issued back to back, 700-900 with the bookkeeping and barrier checks in
+    // between).  So the next k-block's bookkeeping and a one-shot probe of its full barrier
+    // run after the third MMA of the current k-block, while the pipe still has work; the
+    // thread blocks on a barrier only when that probe failed or a pass begins.
     if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      uint32_t tphase[2] = {0, 0};
-      int buf = 0;
-      bool ok = true;
-      for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
-        Seq q;
-        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
-          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-          if (q.pass_first()) {
-            ok = mbar_wait(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, P.err);
-            if (!ok) break;
-            tc_fence_after();
-          }
-          ok = mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err);
-          if (!ok) break;
-          tc_fence_after();
-          const uint32_t sa = smem_u32(smem + (size_t)stage * STAGE_BYTES);
-          const uint64_t ad = smem_desc(sa), bd = smem_desc(sa + A_BYTES);
-#pragma unroll
-          for (int kk = 0; kk < KB / 32; ++kk)  // K = 32 e4m3 = 32 bytes per MMA: +2 in the 16-byte address field
-            mma_f8(d_tmem, ad + 2 * kk, bd + 2 * kk, (q.pass_first() && kk == 0) ? 0u : 1u);
-          // the stage is free (in every CTA of the cluster) when these MMAs have read it
-          if (CM > 1) mma_commit_mc(empty0 + 8 * stage, MASK);
-          else mma_commit(empty0 + 8 * stage);
-          if (q.pass_last()) {
-            mma_commit(tfull0 + 8 * buf);
-            tphase[buf] ^= 1;
-            buf ^= 1;
-          }
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
-          }
+      static_assert(KB / 32 == 4, "four K = 32 MMAs per k-block");
+      constexpr uint64_t STAGE_STEP = (uint64_t)(STAGE_BYTES >> 4);  // descriptor address field per stage
+      const uint32_t sa0 = smem_u32(smem);
+      const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + A_BYTES);
+      MmaCursor cur;
+      cur.start(cluster_id, total_ctiles, P.s, P.nkb);
+      int stage = 0, buf = 0;
+      uint32_t phase = 0, tph = 0;  // tph bit b: phase of accumulator b's full barrier
+      uint64_t ad = ad0, bd = bd0;
+      bool ok = cur.valid;
+      bool first = cur.q.pass_first(), last = cur.q.pass_last();
+      if (ok) ok = mbar_wait(tempty0, 1, abort_flag, P.err);  // first pass: buffer 0 is free
+      if (ok) ok = mbar_wait(full0, 0, abort_flag, P.err);
+      tc_fence_after();
+      while (ok) {
+        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+        // K = 32 e4m3 = 32 bytes per MMA: +2 in the 16-byte address field
+        mma_f8(d_tmem, ad, bd, first ? 0u : 1u);
+        mma_f8(d_tmem, ad + 2, bd + 2, 1u);
+        mma_f8(d_tmem, ad + 4, bd + 4, 1u);
+        // ---- next k-block, while two MMAs are still queued
+        cur.next(num_clusters, total_ctiles, P.s, P.nkb);
+        const bool nvalid = cur.valid;
+        const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
+        const int nstage = stage + 1 == STAGES ? 0 : stage + 1;
+        const uint32_t nphase = nstage == 0 ? phase ^ 1u : phase;
+        const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
+        const bool ready = nvalid && !nfirst && mbar_try_wait(full0 + 8 * nstage, nphase);
+        mma_f8(d_tmem, ad + 6, bd + 6, 1u);
+        // the stage is free (in every CTA of the cluster) when these MMAs have read it
+        if (CM > 1) mma_commit_mc(empty0 + 8 * stage, MASK);
+        else mma_commit(empty0 + 8 * stage);
+        if (last) {
+          mma_commit(tfull0 + 8 * buf);
+          tph ^= 1u << buf;
+          buf ^= 1;
         }
+        stage = nstage;
+        phase = nphase;
+        ad = nad;
+        bd = nbd;
+        first = nfirst;
+        last = nlast;
+        if (ready) {  // fast path: the next stage is loaded and no pass begins
+          tc_fence_after();
+          continue;
+        }
+        if (!nvalid) break;
+        if (first) {
+          ok = mbar_wait(tempty0 + 8 * buf, ((tph >> buf) & 1u) ^ 1u, abort_flag, P.err);
+          if (!ok) break;
+        }
+        ok = mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err);
+        if (!ok) break;
+        tc_fence_after();
       }
       // wait (bounded) for the MMAs in flight before TMEM is freed
       for (int b = 0; b < 2; ++b) {
-        (void)mbar_wait(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, P.err);
+        (void)mbar_wait(tempty0 + 8 * buf, ((tph >> buf) & 1u) ^ 1u, abort_flag, P.err);
         buf ^= 1;
       }
     }
@@ -653,44 +699,62 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer (leader)
+    // issue order as in oz_gemm_tc: the next k-block's bookkeeping between its third and fourth MMA
     if (lane == 0 && rank == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
-      uint32_t tphase[2] = {0, 0};
-      int buf = 0;
-      bool ok = true;
-      for (int ct = pair_id; ct < total_tiles && ok; ct += num_pairs) {
-        Seq q;
-        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
-          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-          if (q.pass_first()) {
-            ok = mbar_wait_pair<true>(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, peer_abort, P.err);
-            if (!ok) break;
-            tc_fence_after();
-          }
-          ok = mbar_wait_pair<false>(full0 + 8 * stage, phase, abort_flag, peer_abort, P.err);
-          if (!ok) break;
-          tc_fence_after();
-          const uint32_t sa = smem_u32(smem + (size_t)stage * PAIR_STAGE_BYTES);
-          const uint64_t ad = smem_desc(sa), bd = smem_desc(sa + PAIR_A_BYTES);
-#pragma unroll
-          for (int kk = 0; kk < KB / 32; ++kk)
-            mma_f8_pair(d_tmem, ad + 2 * kk, bd + 2 * kk, (q.pass_first() && kk == 0) ? 0u : 1u);
-          mma_commit_pair(empty0 + 8 * stage, BOTH);  // the stage is free in both CTAs
-          if (q.pass_last()) {
-            mma_commit_pair(tfull0 + 8 * buf, BOTH);
-            tphase[buf] ^= 1;
-            buf ^= 1;
-          }
-          if (++stage == PAIR_STAGES) {
-            stage = 0;
-            phase ^= 1;
-          }
+      constexpr uint64_t STAGE_STEP = (uint64_t)(PAIR_STAGE_BYTES >> 4);
+      const uint32_t sa0 = smem_u32(smem);
+      const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + PAIR_A_BYTES);
+      MmaCursor cur;
+      cur.start(pair_id, total_tiles, P.s, P.nkb);
+      int stage = 0, buf = 0;
+      uint32_t phase = 0, tph = 0;
+      uint64_t ad = ad0, bd = bd0;
+      bool ok = cur.valid;
+      bool first = cur.q.pass_first(), last = cur.q.pass_last();
+      if (ok) ok = mbar_wait_pair<true>(tempty0, 1, abort_flag, peer_abort, P.err);
+      if (ok) ok = mbar_wait_pair<false>(full0, 0, abort_flag, peer_abort, P.err);
+      tc_fence_after();
+      while (ok) {
+        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+        mma_f8_pair(d_tmem, ad, bd, first ? 0u : 1u);
+        mma_f8_pair(d_tmem, ad + 2, bd + 2, 1u);
+        mma_f8_pair(d_tmem, ad + 4, bd + 4, 1u);
+        cur.next(num_pairs, total_tiles, P.s, P.nkb);
+        const bool nvalid = cur.valid;
+        const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
+        const int nstage = stage + 1 == PAIR_STAGES ? 0 : stage + 1;
+        const uint32_t nphase = nstage == 0 ? phase ^ 1u : phase;
+        const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
+        const bool ready = nvalid && !nfirst && mbar_try_wait(full0 + 8 * nstage, nphase);
+        mma_f8_pair(d_tmem, ad + 6, bd + 6, 1u);
+        mma_commit_pair(empty0 + 8 * stage, BOTH);  // the stage is free in both CTAs
+        if (last) {
+          mma_commit_pair(tfull0 + 8 * buf, BOTH);
+          tph ^= 1u << buf;
+          buf ^= 1;
         }
+        stage = nstage;
+        phase = nphase;
+        ad = nad;
+        bd = nbd;
+        first = nfirst;
+        last = nlast;
+        if (ready) {
+          tc_fence_after();
+          continue;
+        }
+        if (!nvalid) break;
+        if (first) {
+          ok = mbar_wait_pair<true>(tempty0 + 8 * buf, ((tph >> buf) & 1u) ^ 1u, abort_flag, peer_abort, P.err);
+          if (!ok) break;
+        }
+        ok = mbar_wait_pair<false>(full0 + 8 * stage, phase, abort_flag, peer_abort, P.err);
+        if (!ok) break;
+        tc_fence_after();
       }
       // both accumulators released by both CTAs: no MMA is in flight when TMEM is freed
       for (int b = 0; b < 2; ++b) {
-        (void)mbar_wait_pair<true>(tempty0 + 8 * buf, tphase[buf] ^ 1, abort_flag, peer_abort, P.err, false);
+        (void)mbar_wait_pair<true>(tempty0 + 8 * buf, ((tph >> buf) & 1u) ^ 1u, abort_flag, peer_abort, P.err, false);
         buf ^= 1;
       }
     }
