@@ -36,7 +36,15 @@ sys.path.insert(0, str(ROOT / "tiled-mm_gb300"))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 # measured on this machine's GB300 with the repository's own probes (mma.sync loops, CUDA events)
-MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 151.2, "dmma_f64_tflops": 1.054, "dfma_f64_tflops": 1.012}
+# Instruction-rate ceilings on this machine's GB300, measured by tiled-mm_gb300/peaks/engine_rates.cu
+# (dmma, imma; tcgen05 e4m3 M128 N256 K32 back to back from shared memory) and the vendor library's
+# dense e4m3 GEMM (tiled-mm_gb300/peaks/cublaslt_e4m3.py, 8192^3); summarised in
+# profiles/engine_rates.md.
+MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 157.9, "dmma_f64_tflops": 1.099,
+                         "tcgen05_e4m3_tflops": 4847.2, "cublaslt_e4m3_tflops": 3948.0}
+# DRAM bytes (read + write) per launch of the slice-product kernel, from one ncu capture of the
+# workload's own command (profiles/oz_gemm_tc_ozaki32768.md): (workload, tiles, slices) -> bytes
+MEASURED_TRAFFIC = {("ozaki32768", (32768, 32768, 16384), 11): 2.871e12}
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
@@ -243,6 +251,7 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     # inputs (8.6 GB per operand at the default workload) are far larger than the 126 MB L2
     times = []
     barrier(dist)
+    ctx.set_kernel_timing(True)  # events on the engine's stream around each engine launch
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for _ in range(args.steps):
             Cd.copy_(C0)  # restore C (also evicts L2); outside the event-timed region
@@ -251,6 +260,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             ev[1].record(stream)
             ev[1].synchronize()
             times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+    kernel_seconds, kernel_launches = ctx.kernel_time()
+    ctx.set_kernel_timing(False)
     barrier(dist)
     t_step = max_over_ranks(dist, float(np.mean(times)))
     result["value"] = world * flops / t_step / 1e12
@@ -258,9 +269,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     result["clocks"] = clk.summary()
     result["gpu_launches"] = launches_per_step * args.steps
 
-    # ---- dominant kernel: per-launch time with CUDA events on its stream (one extra run)
-    # the gemm kernel of the engine is the dominant launch; its share comes from the ncu launch list
+    # ---- dominant kernel: the engine launches of the timed steps, each bracketed by CUDA events
     result["device_step_seconds"] = t_step
+    result["engine_kernel"] = {"launches": kernel_launches, "ms_per_launch": 1e3 * kernel_seconds / max(kernel_launches, 1),
+                               "share_of_step": kernel_seconds / (t_step * args.steps)}
 
     # ---- error metric of this path's result (sampled entries, compensated dot products on the host)
     Cd.copy_(C0)
@@ -344,17 +356,27 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         lowp_ops = pairs * flops
         if eng["engine"] == "imma":
             peak = MEASURED_ENGINE_PEAKS["imma_s8_tops"]
-            src = "measured on this pool's GB300 by the repository's mma.sync s8 probe"
+            src = "mma.sync m16n8k32 s8 issue rate, tiled-mm_gb300/peaks/engine_rates.cu"
         else:
             bf16 = measured_peaks().get("bf16_tflops") or 1910.1
             peak = 2.0 * bf16
             src = "2 x the measured dense bf16 cuBLAS burst rate in MEASURED_PEAKS.json (e4m3 issues at twice bf16)"
-        achieved = lowp_ops / t_step / 1e12
+        # algorithmic low-precision operations per launch over the average launch duration
+        achieved = lowp_ops * args.steps / kernel_seconds / 1e12
+        traffic = MEASURED_TRAFFIC.get((args.workload, tuple(result["tiles"][:3]), slices))
         result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                              "frac": achieved / peak, "traffic": None,
+                              "frac": achieved / peak, "traffic": traffic,
                               "kernel": "oz_gemm_tc" if eng["engine"] == "tcgen05" else "oz_gemm_imma",
-                              "ops": f"{pairs} slice-pair products x 2mnk (whole step incl. split kernels)",
+                              "ops": f"{pairs} slice-pair products x 2mnk per step, over the engine launches' "
+                                     "event-timed durations",
                               "peak_source": src}
+        if eng["engine"] == "tcgen05":
+            result["roofline"]["frac_of_other_ceilings"] = {
+                "cublaslt_e4m3_gemm": achieved / MEASURED_ENGINE_PEAKS["cublaslt_e4m3_tflops"],
+                "tcgen05_pipe_back_to_back": achieved / MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"]}
+        if traffic:
+            result["roofline"]["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " \
+                                                   "profiles/oz_gemm_tc_ozaki32768.md"
         result["slices"] = slices
         result["slice_pairs"] = pairs
         result["engine"] = eng
@@ -362,9 +384,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             result["calibration"] = calib
     else:
         peak = MEASURED_ENGINE_PEAKS["dmma_f64_tflops"]
-        result["roofline"] = {"bound": "tensor", "achieved": result["value"], "peak": peak, "unit": "TFLOP/s",
-                              "frac": result["value"] / peak, "traffic": None, "kernel": "gemm_f64_dmma",
-                              "peak_source": "measured on this pool's GB300 by the repository's mma.sync probe"}
+        achieved = flops * args.steps / kernel_seconds / 1e12
+        result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                              "frac": achieved / peak, "traffic": None, "kernel": "gemm_f64_dmma",
+                              "peak_source": "mma.sync m16n8k4 f64 issue rate, tiled-mm_gb300/peaks/engine_rates.cu"}
     return result
 
 

@@ -220,6 +220,14 @@ typedef struct tmm_stats {
 
 int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);
 
+/* Timing of the engine kernels (the tile GEMM of the native path, the slice-product
+ * kernel of the Ozaki path), for profiling; no counterpart in the reference.  While on,
+ * every engine launch is bracketed by two CUDA events recorded on its stream.
+ * tmm_set_kernel_timing clears the totals; tmm_get_kernel_time waits for the recorded
+ * launches and returns the summed device time (seconds) and the number of launches. */
+int tmm_set_kernel_timing(tmm_context* ctx, int on);
+int tmm_get_kernel_time(tmm_context* ctx, double* seconds, uint64_t* launches);
+
 /* Message of the last failure of this context (ctx == NULL: of the calling
  * thread's last context-free call).  Never NULL. */
 const char* tmm_last_error(tmm_context* ctx);

@@ -220,6 +220,26 @@ def test_device_entry_matches_host_entry(tmm):
     np.testing.assert_array_equal(dc.cpu().numpy(), host)
 
 
+def test_kernel_timing_counts_engine_launches(tmm):
+    """tmm_set_kernel_timing / tmm_get_kernel_time: one event-timed interval per engine launch
+    while on (native tile GEMMs here: 2 x 2 C tiles x 2 k-tiles), none while off, and no effect
+    on results."""
+    rng = np.random.default_rng(12)
+    m, n, k = 300, 260, 200
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k)
+    ctx = tmm.make_context(np.float64, 2, 150, 130, 100)
+    ctx.set_tile_policy(tmm.TILE_POLICY_FIXED)
+    plain = run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
+    ctx.set_kernel_timing(True)
+    timed = run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
+    sec, launches = ctx.kernel_time()
+    assert launches == 8 and sec > 0
+    np.testing.assert_array_equal(timed, plain)
+    ctx.set_kernel_timing(False)
+    run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
+    assert ctx.kernel_time() == (0.0, 0)
+
+
 def test_device_generator_matches_host(tmm):
     torch = pytest.importorskip("torch")
     rows, cols, ld = 257, 33, 300

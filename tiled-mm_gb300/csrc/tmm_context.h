@@ -99,6 +99,13 @@ struct tmm_context {
 
   tmm::OzakiState* oz = nullptr;
 
+  // optional timing of the engine kernels (tmm_set_kernel_timing): event pairs recorded
+  // on the launching stream around each launch, summed by tmm_get_kernel_time
+  bool ktime = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_pending, kt_free;
+  double kt_seconds = 0.0;
+  uint64_t kt_launches = 0;
+
   tmm_stats stats{};
   std::string last_error;
 };

@@ -105,10 +105,42 @@ struct DeviceGuard {
   }
 };
 
+// Brackets one engine launch with a pair of events on its stream when kernel timing is on.
+struct KernelTimer {
+  tmm_context* ctx;
+  cudaStream_t s;
+  std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+  KernelTimer(tmm_context* c, cudaStream_t st) : ctx(c), s(st) {
+    if (!ctx->ktime) return;
+    if (!ctx->kt_free.empty()) {
+      ev = ctx->kt_free.back();
+      ctx->kt_free.pop_back();
+    } else {
+      if (cudaEventCreate(&ev.first) != cudaSuccess) {
+        ev = {nullptr, nullptr};
+        return;
+      }
+      if (cudaEventCreate(&ev.second) != cudaSuccess) {
+        cudaEventDestroy(ev.first);
+        ev = {nullptr, nullptr};
+        return;
+      }
+    }
+    cudaEventRecord(ev.first, s);
+  }
+  void done() {
+    if (!ev.first) return;
+    cudaEventRecord(ev.second, s);
+    ctx->kt_pending.push_back(ev);
+    ev = {nullptr, nullptr};
+  }
+};
+
 int launch_tile_gemm(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
                      const void* A, int64_t lda, const void* B, int64_t ldb, const void* beta, void* C,
                      int64_t ldc, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
+  KernelTimer timer(ctx, s);
   switch (ctx->dtype) {
     case TMM_FLOAT:
       e = k == 0 ? tmm::launch_scale_f32(m, n, *(const float*)beta, (float*)C, ldc, s)
@@ -130,6 +162,7 @@ int launch_tile_gemm(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int
                  : tmm::launch_gemm_c64(opa, opb, m, n, k, *(const tmm::cplxd*)alpha, (const tmm::cplxd*)A, lda,
                                         (const tmm::cplxd*)B, ldb, *(const tmm::cplxd*)beta, (tmm::cplxd*)C, ldc, s);
   }
+  timer.done();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "tile kernel launch");
   ctx->stats.kernels++;
   return TMM_SUCCESS;
@@ -277,6 +310,11 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   if (ctx->batch_aux) cudaStreamDestroy(ctx->batch_aux);
   if (ctx->batch_fork) cudaEventDestroy(ctx->batch_fork);
   if (ctx->batch_join) cudaEventDestroy(ctx->batch_join);
+  for (auto* v : {&ctx->kt_pending, &ctx->kt_free})
+    for (auto& ev : *v) {
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
   ctx->batch_arena.release();
   ctx->batch_meta.release();
   for (auto s : ctx->streams) cudaStreamDestroy(s);
@@ -407,6 +445,37 @@ extern "C" int tmm_set_memory_limit(tmm_context* ctx, size_t bytes) {
 extern "C" int tmm_get_stats(tmm_context* ctx, tmm_stats* st) {
   if (!ctx || !st) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_stats: null argument");
   *st = ctx->stats;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_set_kernel_timing(tmm_context* ctx, int on) {
+  if (!ctx) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_kernel_timing: null context");
+  DeviceGuard dg(ctx->device);
+  for (auto& ev : ctx->kt_pending) {  // drop what was recorded so far
+    cudaEventSynchronize(ev.second);
+    ctx->kt_free.push_back(ev);
+  }
+  ctx->kt_pending.clear();
+  ctx->kt_seconds = 0.0;
+  ctx->kt_launches = 0;
+  ctx->ktime = on != 0;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_kernel_time(tmm_context* ctx, double* seconds, uint64_t* launches) {
+  if (!ctx || !seconds) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_kernel_time: null argument");
+  DeviceGuard dg(ctx->device);
+  for (auto& ev : ctx->kt_pending) {
+    TMM_CUDA(ctx, cudaEventSynchronize(ev.second));
+    float ms = 0.0f;
+    TMM_CUDA(ctx, cudaEventElapsedTime(&ms, ev.first, ev.second));
+    ctx->kt_seconds += 1e-3 * (double)ms;
+    ctx->kt_launches++;
+    ctx->kt_free.push_back(ev);
+  }
+  ctx->kt_pending.clear();
+  *seconds = ctx->kt_seconds;
+  if (launches) *launches = ctx->kt_launches;
   return TMM_SUCCESS;
 }
 
@@ -695,8 +764,10 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         } else {
           tmm::OzakiSplit va = tmm::ozaki_split_view(SA.ptr, mi, kk, P.slices, P.engine);
           tmm::OzakiSplit vb = tmm::ozaki_split_view(SB.ptr, nj, kk, P.slices, P.engine);
+          KernelTimer timer(ctx, s);
           cudaError_t e = tmm::ozaki_gemm(va, vb, mi, nj, *(const double*)alpha, *(const double*)beta, kt == 0,
                                           (double*)ct, ldct, P.engine, oz_workspace(ctx, sidx), oz_error_word(ctx), s);
+          timer.done();
           if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki gemm launch");
           ctx->stats.kernels++;
         }
@@ -867,9 +938,12 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
       const double* bb = opb == tmm::OP_N ? (const double*)b + k0 : (const double*)b + k0 * ld_b;
       cudaError_t e = tmm::ozaki_split(ab, ld_a, opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, m, kk, va, s);
       if (e == cudaSuccess) e = tmm::ozaki_split(bb, ld_b, opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, n, kk, vb, s);
-      if (e == cudaSuccess)
+      if (e == cudaSuccess) {
+        KernelTimer timer(ctx, s);
         e = tmm::ozaki_gemm(va, vb, m, n, *(const double*)alpha, *(const double*)beta, kt == 0, (double*)c, ld_c,
                             ctx->oz_engine, oz_workspace(ctx, 0), oz_error_word(ctx), s);
+        timer.done();
+      }
       if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki device gemm launch");
       ctx->stats.kernels += 3;
     }

@@ -1,0 +1,235 @@
+// Issue-rate probes for the instructions the library's engines are built on, on one GB300:
+//   dmma    mma.sync m16n8k4 f64 (native FP64 tile kernel)
+//   imma    mma.sync m16n8k32 s8 -> s32 (IMMA Ozaki engine)
+//   tcgen05 tcgen05.mma.cta_group::1.kind::f8f6f4, M128 N256 K32, e4m3 operands resident in shared
+//           memory, issued back to back from one thread (tcgen05 Ozaki engine, pipe ceiling)
+// Every CTA runs a fixed number of iterations; the tcgen05 probe's one wait is bounded by %globaltimer.
+//
+//   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -o engine_rates engine_rates.cu
+//   ./engine_rates        # one JSON line per probe
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#define CK(x)                                                                     \
+  do {                                                                            \
+    cudaError_t e_ = (x);                                                         \
+    if (e_ != cudaSuccess) {                                                      \
+      printf("{\"error\": \"%s: %s\"}\n", #x, cudaGetErrorString(e_));            \
+      return 1;                                                                   \
+    }                                                                             \
+  } while (0)
+
+__global__ void dmma_loop(double* out, int iters) {
+  double acc[4][4] = {};
+  const double a0 = threadIdx.x * 1e-3, a1 = a0 + 1.0, b0 = 0.5;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      asm volatile("mma.sync.aligned.m16n8k4.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+                   : "+d"(acc[c][0]), "+d"(acc[c][1]), "+d"(acc[c][2]), "+d"(acc[c][3])
+                   : "d"(a0), "d"(a1), "d"(b0));
+  }
+  double s = 0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) s += acc[i][j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void imma_loop(int* out, int iters) {
+  int acc[4][4] = {};
+  const int a0 = 0x01020304 + threadIdx.x, a1 = a0 ^ 0x05050505, a2 = a0 + 7, a3 = a1 + 9, b0 = 0x01010101, b1 = 0x02020202;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      asm volatile(
+          "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+          : "+r"(acc[c][0]), "+r"(acc[c][1]), "+r"(acc[c][2]), "+r"(acc[c][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  int s = 0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) s += acc[i][j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// K-major, 128-byte swizzle, 8-row groups 1024 bytes apart (the engine's operand layout)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+         ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ bool try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok)
+               : "r"(bar), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+
+// One CTA per SM; 4 operand stages of 16 KB (A, 128 x 128 bytes) + 32 KB (B, 256 x 128 bytes) filled
+// with e4m3 1.0; `kblocks` k-blocks of 4 MMAs into two alternating TMEM accumulators.
+// mode 0: back to back, the next stage's descriptors computed between the third and fourth MMA;
+// mode 1: descriptors, accumulator and flags computed after the fourth MMA, then a check of a
+//         barrier that has already completed (up to 256 probes), as a straightforward loop does;
+// mode 2: mode 0 plus a one-shot probe of that barrier between the third and fourth MMA.
+__global__ void __launch_bounds__(128, 1) tcgen05_loop(int kblocks, int mode, long long* cycles, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t fin, done0;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < 4 * 49152 / 4; i += blockDim.x) ((uint32_t*)smem)[i] = 0x38383838u;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&fin)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done0)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&done0)) : "memory");  // phase 0 done
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)), "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tslot;
+  constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  if (warp == 0 && lane == 0) {
+    const uint64_t ad0 = smem_desc(smem_u32(smem)), bd0 = smem_desc(smem_u32(smem + 16384));
+    const long long t0 = clock64();
+    uint64_t ad = ad0, bd = bd0;
+    const uint32_t d0 = smem_u32(&done0);
+    if (mode == 1) {
+      for (int kb = 0; kb < kblocks; ++kb) {
+        for (int i = 0; i < 256; ++i)
+          if (try_wait(d0, 0)) break;
+        const int st = kb & 3;
+        const uint64_t a = smem_desc(smem_u32(smem + st * 49152)), b = smem_desc(smem_u32(smem + st * 49152 + 16384));
+        const uint32_t d = tmem + (uint32_t)(((kb / 512) & 1) * 256);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint32_t acc = (kb % 512 == 0 && kk == 0) ? 0u : 1u;
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+                       ::"r"(d), "l"(a + 2 * kk), "l"(b + 2 * kk), "r"(IDESC), "r"(acc));
+        }
+      }
+    }
+    for (int kb = 0; mode != 1 && kb < kblocks; ++kb) {
+      const uint32_t d = tmem + (uint32_t)(((kb >> 9) & 1) * 256);
+      const uint32_t acc0 = (kb & 511) ? 1u : 0u;
+      asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+                   ::"r"(d), "l"(ad), "l"(bd), "r"(IDESC), "r"(acc0));
+      asm volatile("tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 2), "l"(bd + 2), "r"(IDESC));
+      asm volatile("tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 4), "l"(bd + 4), "r"(IDESC));
+      const bool wrap = (kb & 3) == 3;
+      const uint64_t nad = wrap ? ad0 : ad + (49152 >> 4), nbd = wrap ? bd0 : bd + (49152 >> 4);
+      if (mode == 2 && !try_wait(d0, 0)) atomicOr(err, 2);
+      asm volatile("tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 6), "l"(bd + 6), "r"(IDESC));
+      ad = nad;
+      bd = nbd;
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&fin)) : "memory");
+    uint64_t g0, g1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+    while (true) {
+      uint32_t ok;
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                   : "=r"(ok) : "r"(smem_u32(&fin)) : "memory");
+      if (ok) break;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+      if (g1 - g0 > 1000000000ull) {
+        atomicOr(err, 1);
+        break;
+      }
+    }
+    cycles[blockIdx.x] = clock64() - t0;
+  }
+  __syncwarp();
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+static float time_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+int main() {
+  int dev = 0, sms = 0, clk_khz = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, dev));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  void* out = nullptr;
+  CK(cudaMalloc(&out, (size_t)sms * 8 * 256 * sizeof(double)));
+  {  // DMMA: 8 warps per CTA, 2 CTAs per SM
+    const int iters = 20000, block = 256, grid = sms * 2;
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(e0));
+      dmma_loop<<<grid, block>>>((double*)out, iters);
+      CK(cudaEventRecord(e1));
+      CK(cudaEventSynchronize(e1));
+      const double flop = (double)grid * (block / 32) * iters * 4 * (2.0 * 16 * 8 * 4);
+      if (rep) printf("{\"probe\": \"dmma_m16n8k4_f64\", \"tflops\": %.3f}\n", flop / time_ms(e0, e1) / 1e9);
+    }
+  }
+  {  // IMMA s8
+    const int iters = 20000, block = 256, grid = sms * 2;
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(e0));
+      imma_loop<<<grid, block>>>((int*)out, iters);
+      CK(cudaEventRecord(e1));
+      CK(cudaEventSynchronize(e1));
+      const double ops = (double)grid * (block / 32) * iters * 4 * (2.0 * 16 * 8 * 32);
+      if (rep) printf("{\"probe\": \"imma_m16n8k32_s8\", \"tops\": %.3f}\n", ops / time_ms(e0, e1) / 1e9);
+    }
+  }
+  for (int mode = 0; mode < 3; ++mode) {  // tcgen05 e4m3 pipe
+    const int kblocks = 20000;
+    const int smem = 4 * 49152 + 1024;
+    long long* cyc = nullptr;
+    int* err = nullptr;
+    CK(cudaMalloc(&cyc, sms * sizeof(long long)));
+    CK(cudaMalloc(&err, sizeof(int)));
+    CK(cudaMemset(err, 0, sizeof(int)));
+    CK(cudaFuncSetAttribute(tcgen05_loop, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(e0));
+      tcgen05_loop<<<sms, 128, smem>>>(kblocks, mode, cyc, err);
+      CK(cudaEventRecord(e1));
+      CK(cudaEventSynchronize(e1));
+      if (!rep) continue;
+      long long h[512];
+      int herr = 0;
+      const int n = sms < 512 ? sms : 512;
+      CK(cudaMemcpy(h, cyc, n * sizeof(long long), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+      double c = 0;
+      for (int i = 0; i < n; ++i) c += (double)h[i];
+      c /= n;
+      const double flop = (double)sms * kblocks * (2.0 * 128 * 256 * 128);
+      static const char* form[3] = {"back_to_back", "bookkeeping_after_4th_mma", "probe_between_3rd_and_4th"};
+      printf("{\"probe\": \"tcgen05_f8f6f4_m128n256k32\", \"issue_loop\": \"%s\", \"tflops\": %.1f, "
+             "\"cycles_per_kblock\": %.1f, \"flop_per_clk_per_sm\": %.0f, \"tflops_at_max_clock\": %.1f, "
+             "\"wait_error\": %d}\n",
+             form[mode], flop / time_ms(e0, e1) / 1e9, c / kblocks, 2.0 * 128 * 256 * 128 * kblocks / c,
+             2.0 * 128 * 256 * 128 * kblocks / c * sms * (clk_khz * 1e3) / 1e12, herr);
+    }
+    CK(cudaFree(cyc));
+    CK(cudaFree(err));
+  }
+  return 0;
+}

@@ -74,6 +74,8 @@ SIGNATURES = {
     "tmm_set_tile_policy": (_ci, [_p, _ci]),
     "tmm_set_memory_limit": (_ci, [_p, _sz]),
     "tmm_get_stats": (_ci, [_p, _p]),
+    "tmm_set_kernel_timing": (_ci, [_p, _ci]),
+    "tmm_get_kernel_time": (_ci, [_p, _p, _p]),
     "tmm_last_error": (C.c_char_p, [_p]),
     "tmm_status_string": (C.c_char_p, [_ci]),
     "tmm_malloc_pinned": (_ci, [_sz, C.POINTER(_p)]),
@@ -252,6 +254,16 @@ class MMHandle:
 
     def set_memory_limit(self, nbytes: int) -> None:
         _check(_lib.tmm_set_memory_limit(self._h, nbytes), self._h)
+
+    def set_kernel_timing(self, on: bool = True) -> None:
+        """Bracket every engine kernel launch with CUDA events on its stream (clears the totals)."""
+        _check(_lib.tmm_set_kernel_timing(self._h, int(bool(on))), self._h)
+
+    def kernel_time(self) -> tuple[float, int]:
+        """(device seconds, launches) of the engine kernels since set_kernel_timing(True)."""
+        sec, n = C.c_double(), C.c_uint64()
+        _check(_lib.tmm_get_kernel_time(self._h, C.byref(sec), C.byref(n)), self._h)
+        return sec.value, n.value
 
     def stats(self) -> dict:
         s = Stats()
