@@ -42,14 +42,15 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 # profiles/engine_rates.md.
 MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 157.9, "dmma_f64_tflops": 1.099,
                          "tcgen05_e4m3_tflops": 4847.2, "cublaslt_e4m3_tflops": 3948.0}
-# DRAM bytes (read + write) per launch of the slice-product kernel, from one ncu capture of the
-# workload's own command (profiles/oz_gemm_tc_ozaki32768.md): (workload, tiles, slices) -> bytes
+# DRAM bytes (read + write) per launch of the slice-product kernel on the device-resident path,
+# from one ncu capture of the workload's own command (profiles/oz_gemm_tc_ozaki32768.md):
+# (workload, launch m, n, k tile, slices) -> bytes
 MEASURED_TRAFFIC = {("ozaki32768", (32768, 32768, 16384), 11): 2.871e12}
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
-                       path="ozaki", tiles=(32768, 32768, 16384), streams=2,
-                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20], k tiles of 16384"),
+                       path="ozaki", tiles=(16384, 16384, 16384), streams=2,
+                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20], tiles 16384^3"),
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
@@ -328,22 +329,35 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         hctx.set_ozaki_engine(w["engine"])
     copy_back = w.get("copy_back", True)
     e2e_times = []
-    for it in range(max(1, args.e2e_warmup) + args.e2e_steps):
-        if c_init is not None:
-            hc[:] = c_init
-        t0 = time.perf_counter()
+
+    def e2e_call():
         tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], hc, m,
                  pin_host_buffers=w.get("pin", False), copy_c_back=copy_back)
-        t1 = time.perf_counter()
-        if it >= max(1, args.e2e_warmup):
-            e2e_times.append(t1 - t0)
+
+    for _ in range(max(1, args.e2e_warmup)):
+        if c_init is not None:
+            hc[:] = c_init
+        e2e_call()
+    hctx.set_kernel_timing(True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as e2e_clk:
+        for _ in range(args.e2e_steps):
+            if c_init is not None:
+                hc[:] = c_init
+            t0 = time.perf_counter()
+            e2e_call()
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_kernel_s, _ = hctx.kernel_time()
+    hctx.set_kernel_timing(False)
     st = hctx.stats()
     t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
     result["e2e"] = {"value": world * flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
                      "d2h_bytes_per_step": st["d2h_bytes"], "seconds_per_step": t_e2e,
                      "host_buffers": ("pageable, registered inside each call" if w.get("pin") else "pageable")
                      if pageable else "pinned (cudaHostAlloc)",
-                     "copy_c_back": copy_back, "steps": args.e2e_steps}
+                     "copy_c_back": copy_back, "steps": args.e2e_steps,
+                     "step_seconds": [round(x, 4) for x in e2e_times],
+                     "engine_kernel_seconds_per_step": e2e_kernel_s / max(1, args.e2e_steps),
+                     "clocks": e2e_clk.summary()}
     result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"], st["n_streams"]]
     result["e2e_tiles_loaded"] = st["tiles_loaded"]
     hctx.close()
@@ -363,10 +377,13 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             src = "2 x the measured dense bf16 cuBLAS burst rate in MEASURED_PEAKS.json (e4m3 issues at twice bf16)"
         # algorithmic low-precision operations per launch over the average launch duration
         achieved = lowp_ops * args.steps / kernel_seconds / 1e12
-        traffic = MEASURED_TRAFFIC.get((args.workload, tuple(result["tiles"][:3]), slices))
+        # the device-resident path launches the engine on all of C per k tile
+        launch = (m, n, min(k, w["tiles"][2]))
+        traffic = MEASURED_TRAFFIC.get((args.workload, launch, slices))
         result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": traffic,
                               "kernel": "oz_gemm_tc" if eng["engine"] == "tcgen05" else "oz_gemm_imma",
+                              "launch_mnk": list(launch),
                               "ops": f"{pairs} slice-pair products x 2mnk per step, over the engine launches' "
                                      "event-timed durations",
                               "peak_source": src}
@@ -500,7 +517,7 @@ def main() -> None:
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--skip-native", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--tiles", default="", help="tile_m,tile_n,tile_k of the context (overrides the workload's)")
     args = ap.parse_args()

@@ -607,7 +607,7 @@ struct HostMat {
 // last reader.  Ozaki tiles are staged raw, then split on the prep stream.
 int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t key, const HostMat& h,
                int64_t r0, int64_t c0, int64_t rr, int64_t cc, bool lines_are_rows, int* out_slot,
-               int* staging_turn) {
+               int* staging_turn, cudaStream_t split_stream) {
   int idx = cache.find(key);
   if (idx >= 0) {
     cache.slots[idx].stamp = ++cache.clock;
@@ -625,25 +625,28 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
                                     (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));
   } else {
-    // raw tile -> staging buffer (ring of 3) on the copy stream; split -> slot on the prep stream
+    // raw tile -> staging buffer (ring of 3) on the copy stream; split -> slot on the stream of
+    // the tile's first consumer, after the kernels already queued there: split CTAs resident
+    // beside the persistent slice-product kernel would take issue slots from its single-thread
+    // MMA issuer, and the split is ~3 % of the work, so running it concurrently gains little
     int turn = (*staging_turn)++ % 3;
     char* stage = (char*)ctx->staging.ptr + (size_t)turn * ((P.staging_bytes + 255) / 256 * 256);
     TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->staging_free[turn], 0));
     TMM_CUDA(ctx, cudaMemcpy2DAsync(stage, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
                                     (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));  // reused below as "staged"
-    TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->prep, s.ready, 0));
-    if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->prep, s.last_use, 0));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.ready, 0));
+    if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.last_use, 0));
     // lines along k: for A (lines = rows of op(A)); for B (lines = columns of op(B))
     int64_t lines = lines_are_rows ? rr : cc;   // stored orientation resolved by caller
     int64_t kk = lines_are_rows ? cc : rr;
     Op t = lines_are_rows ? tmm::OP_N : tmm::OP_T;
     tmm::OzakiSplit v = tmm::ozaki_split_view(s.ptr, lines, kk, P.slices, P.engine);
-    cudaError_t e = tmm::ozaki_split((const double*)stage, rr, t, lines, kk, v, ctx->prep);
+    cudaError_t e = tmm::ozaki_split((const double*)stage, rr, t, lines, kk, v, split_stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "ozaki split launch");
     ctx->stats.kernels++;
-    TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->prep));
-    TMM_CUDA(ctx, cudaEventRecord(ctx->staging_free[turn], ctx->prep));
+    TMM_CUDA(ctx, cudaEventRecord(s.ready, split_stream));
+    TMM_CUDA(ctx, cudaEventRecord(ctx->staging_free[turn], split_stream));
   }
   ctx->stats.h2d_bytes += (uint64_t)rr * (uint64_t)cc * P.es;
   ctx->stats.tiles_loaded++;
@@ -742,14 +745,14 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         int sa = -1, sb = -1;
         // A tile (i, kt): stored block rows/cols depend on op(A)
         if (P.opa == tmm::OP_N)
-          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, r0, k0, mi, kk, true, &sa, &staging_turn);
+          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, r0, k0, mi, kk, true, &sa, &staging_turn, s);
         else
-          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, k0, r0, kk, mi, false, &sa, &staging_turn);
+          st = fetch_tile(ctx, P, ctx->cache_a, i * P.ntk + kt, A, k0, r0, kk, mi, false, &sa, &staging_turn, s);
         if (st) return st;
         if (P.opb == tmm::OP_N)
-          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, k0, c0, kk, nj, false, &sb, &staging_turn);
+          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, k0, c0, kk, nj, false, &sb, &staging_turn, s);
         else
-          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, c0, k0, nj, kk, true, &sb, &staging_turn);
+          st = fetch_tile(ctx, P, ctx->cache_b, kt * P.ntn + j, B, c0, k0, nj, kk, true, &sb, &staging_turn, s);
         if (st) return st;
         tmm::Slot& SA = ctx->cache_a.slots[sa];
         tmm::Slot& SB = ctx->cache_b.slots[sb];

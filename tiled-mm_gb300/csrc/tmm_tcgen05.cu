@@ -46,6 +46,8 @@ constexpr int TMEM_COLS = 512;
 constexpr int64_t PASS_BLOCKS = 512;  // 512 * 128 = 65536 k terms per exact FP32 pass
 constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 constexpr unsigned long long WAIT_NS = 1000000000ull;  // one second per wait
+// the epilogue waits a whole pass (tens of microseconds) for an accumulator: park, don't spin
+constexpr uint32_t EPI_WAIT_HINT_NS = 20000;
 
 // ------------------------------------------------------------------ PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -70,13 +72,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait that may park the thread up to hint_ns nanoseconds (it resumes when the phase
+// completes): for waits that are long and not latency-critical
+__device__ __forceinline__ bool mbar_try_wait_hint(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
 // Bounded wait: false after WAIT_NS (error word set) or when another role gave up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err) {
-  for (int i = 0; i < 256; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
+// hint_ns > 0: park between probes (mbar_try_wait_hint) instead of spinning.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
+                                          uint32_t hint_ns = 0) {
+  if (!hint_ns)
+    for (int i = 0; i < 256; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (hint_ns ? mbar_try_wait_hint(bar, parity, hint_ns) : mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
     if (globaltimer() - t0 > WAIT_NS) {
       *abort_flag = 1;
@@ -197,8 +213,12 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t par
 // commits signal their barriers through the async proxy and need only the default.
 template <bool CLUSTER_ACQ>
 __device__ __forceinline__ bool mbar_wait_pair(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                               uint32_t peer_abort, int* err, bool honor_abort = true) {
-  auto probe = [&] { return CLUSTER_ACQ ? mbar_try_wait_cluster(bar, parity) : mbar_try_wait(bar, parity); };
+                                               uint32_t peer_abort, int* err, bool honor_abort = true,
+                                               uint32_t hint_ns = 0) {
+  auto probe = [&] {
+    if (CLUSTER_ACQ) return mbar_try_wait_cluster(bar, parity);
+    return hint_ns ? mbar_try_wait_hint(bar, parity, hint_ns) : mbar_try_wait(bar, parity);
+  };
   for (int i = 0; i < 256; ++i)
     if (probe()) return true;
   const uint64_t t0 = globaltimer();
@@ -538,7 +558,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         if (!q.pass_last()) continue;
         // one lane waits, the warp follows: the TMEM loads below are warp-collective
         int okw = 1;
-        if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err) ? 1 : 0;
+        if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err, EPI_WAIT_HINT_NS) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
         __syncwarp();
         if (!ok) break;
@@ -774,7 +794,9 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
         if (!q.pass_last()) continue;
         int okw = 1;
-        if (lane == 0) okw = mbar_wait_pair<false>(tfull0 + 8 * buf, tphase[buf], abort_flag, peer_abort, P.err) ? 1 : 0;
+        if (lane == 0)
+          okw = mbar_wait_pair<false>(tfull0 + 8 * buf, tphase[buf], abort_flag, peer_abort, P.err, true,
+                                      EPI_WAIT_HINT_NS) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
         __syncwarp();
         if (!ok) break;
