@@ -190,9 +190,10 @@ int tmm_set_path(tmm_context* ctx, int path, int ozaki_slices);
 int tmm_get_path(tmm_context* ctx, int* path, int* ozaki_slices);
 
 /* New: the engine behind TMM_PATH_OZAKI (TMM_OZAKI_IMMA: mma.sync int8 -> int32;
- * TMM_OZAKI_TCGEN05: tcgen05.mma kind::f8f6f4 e4m3 -> FP32 in tensor memory),
- * its k-block (elements) and the k-blocks accumulated exactly between two FP64
- * recombination steps. */
+ * TMM_OZAKI_TCGEN05: tcgen05.mma kind::f8f6f4 e4m3 -> FP32 in tensor memory, the
+ * default of new contexts; the environment variable TMM_OZAKI_ENGINE=imma|tcgen05
+ * overrides it), its k-block (elements) and the k-blocks accumulated exactly between
+ * two FP64 recombination steps. */
 enum tmm_ozaki_engine { TMM_OZAKI_IMMA = 0, TMM_OZAKI_TCGEN05 = 1 };
 int tmm_set_ozaki_engine(tmm_context* ctx, int engine);
 int tmm_get_ozaki_engine(tmm_context* ctx, int* engine, int* k_block, int64_t* pass_blocks);

@@ -36,7 +36,7 @@ int ozaki_default_engine() {
   const char* e = getenv("TMM_OZAKI_ENGINE");
   if (e && strcmp(e, "imma") == 0) return OZ_ENGINE_IMMA;
   if (e && strcmp(e, "tcgen05") == 0) return OZ_ENGINE_TCGEN05;
-  return OZ_ENGINE_IMMA;
+  return OZ_ENGINE_TCGEN05;  // ~10x the IMMA engine's rate on sm_103a
 }
 
 size_t ozaki_split_bytes(int64_t rows, int64_t kk, int slices) {
