@@ -240,6 +240,48 @@ def test_kernel_timing_counts_engine_launches(tmm):
     assert ctx.kernel_time() == (0.0, 0)
 
 
+@pytest.mark.parametrize("copy_c_back", [True, False])
+def test_device_operands_through_tmm_gemm(tmm, oracle, copy_c_back):
+    """tmm_gemm with device pointers (cudaPointerGetAttributes: device memory) runs on the
+    device without the host link: same product as the oracle, nothing copied in or out; with
+    copy_c_back == false the result lands in the full-C buffer and C is left untouched."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(31)
+    m, n, k = 290, 170, 130
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k, pad=3)
+    want, _ = oracle_gemm(oracle, "T", "N", m, n, k, 1.5, a, lda, b, ldb, -0.5, c.copy(), ldc, (m, n, k))
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    ctx = tmm.make_context(np.float64, 2, 128, 128, 64)
+    tmm.gemm(ctx, "T", "N", m, n, k, 1.5, da, lda, db, ldb, -0.5, dc, ldc, True, copy_c_back)
+    st = ctx.stats()
+    assert st["h2d_bytes"] == 0 and st["d2h_bytes"] == 0
+    tol = tol_for(np.float64, k)
+    if copy_c_back:
+        got = dc.cpu().numpy()
+    else:
+        np.testing.assert_array_equal(dc.cpu().numpy(), c)
+        full = np.zeros(m * n)
+        ctx.get_full_device_buffer_c().to_host(full)
+        got = c.copy()
+        got.reshape(n, ldc)[:, :m] = full.reshape(n, m)
+    np.testing.assert_allclose(got, want, rtol=tol, atol=tol)
+
+
+def test_mixed_host_and_device_operands(tmm):
+    """A in device memory, B and C in host memory: the tiled host path copies A's tiles
+    device to device and gives the bits of the all-host call."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(32)
+    m, n, k = 300, 220, 260
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k, pad=1)
+    ctx = tmm.make_context(np.float64, 2, 128, 96, 100)
+    host = run(tmm, ctx, "N", "T", m, n, k, 0.75, a, lda, b, ldb, 1.25, c.copy(), ldc)
+    da = torch.from_numpy(a.copy()).cuda()
+    mixed = c.copy()
+    tmm.gemm(ctx, "N", "T", m, n, k, 0.75, da, lda, b, ldb, 1.25, mixed, ldc)
+    np.testing.assert_array_equal(mixed, host)
+
+
 def test_device_generator_matches_host(tmm):
     torch = pytest.importorskip("torch")
     rows, cols, ld = 257, 33, 300

@@ -167,6 +167,23 @@ def test_out_of_core_ozaki_matches_in_core(tmm, engine):
     np.testing.assert_array_equal(o1, o2)
 
 
+def test_device_operands_through_tmm_gemm_ozaki(tmm, oracle):
+    """Ozaki path, device pointers through the host-pointer call: the device-resident path
+    (k tiles of max_tile_k over all of C), bit for bit the oracle's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(33)
+    m, n, k = 400, 300, 700
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, pad=2, kind="uexp")
+    ctx = ozaki_ctx(tmm, 8, (256, 256, 512), engine="tcgen05")
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    tmm.gemm(ctx, "N", "N", m, n, k, 0.5, da, lda, db, ldb, 2.0, dc, ldc)
+    assert ctx.stats()["h2d_bytes"] == 0
+    eng = ctx.ozaki_engine()
+    want = ozaki_oracle(oracle, "N", "N", m, n, k, 0.5, a, lda, b, ldb, 2.0, c.copy(), ldc, 8, 512, eng["k_block"],
+                        eng["pass_blocks"])
+    np.testing.assert_array_equal(dc.cpu().numpy(), want)
+
+
 def test_ozaki_needs_double(tmm):
     ctx = tmm.make_context(np.float32, 2, 64, 64, 64)
     with pytest.raises(RuntimeError, match="GPU ERROR"):

@@ -191,13 +191,27 @@ struct Pin {
   bool owned = false;
 };
 
+// device or managed memory: the GPU reads it directly (cudaPointerGetAttributes, the
+// query the reference's runtime shim forwards unused: gpu_runtime_api.hpp:223-226)
+bool device_accessible(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes attr;
+  const bool ok = cudaPointerGetAttributes(&attr, p) == cudaSuccess;
+  cudaGetLastError();
+  return ok && (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged);
+}
+
 int pin_range(tmm_context* ctx, const void* p, size_t bytes, Pin* out) {
   out->ptr = nullptr;
   out->owned = false;
   if (!p || bytes == 0) return TMM_SUCCESS;
-  // page-locked already (cudaHostAlloc / cudaMallocHost / an earlier registration): use as is
+  // page-locked already (cudaHostAlloc / cudaMallocHost / an earlier registration), or
+  // device / managed memory: use as is
   cudaPointerAttributes attr;
-  if (cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeHost) return TMM_SUCCESS;
+  if (cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type != cudaMemoryTypeUnregistered) {
+    cudaGetLastError();
+    return TMM_SUCCESS;
+  }
   cudaGetLastError();
   cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
   if (e == cudaSuccess) {
@@ -622,7 +636,7 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
   if (!P.ozaki) {
     if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, s.last_use, 0));
     TMM_CUDA(ctx, cudaMemcpy2DAsync(s.ptr, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
-                                    (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
+                                    (size_t)cc, cudaMemcpyDefault, ctx->h2d));
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));
   } else {
     // raw tile -> staging buffer (ring of 3) on the copy stream; split -> slot on the stream of
@@ -633,7 +647,7 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
     char* stage = (char*)ctx->staging.ptr + (size_t)turn * ((P.staging_bytes + 255) / 256 * 256);
     TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->staging_free[turn], 0));
     TMM_CUDA(ctx, cudaMemcpy2DAsync(stage, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
-                                    (size_t)cc, cudaMemcpyHostToDevice, ctx->h2d));
+                                    (size_t)cc, cudaMemcpyDefault, ctx->h2d));
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));  // reused below as "staged"
     TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.ready, 0));
     if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.last_use, 0));
@@ -733,7 +747,7 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
       }
       if (beta_nz) {  // the C tile is read only when beta != 0 (tiled_mm.cpp:325-330, 425-431)
         TMM_CUDA(ctx, cudaMemcpy2DAsync(ct, (size_t)ldct * P.es, Ch + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es,
-                                        (size_t)ldc * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyHostToDevice, s));
+                                        (size_t)ldc * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDefault, s));
         ctx->stats.h2d_bytes += (uint64_t)mi * (uint64_t)nj * P.es;
       }
       if (P.ntk == 0) {
@@ -782,7 +796,7 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         TMM_CUDA(ctx, cudaEventRecord(cs->done, s));
         TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h, cs->done, 0));
         TMM_CUDA(ctx, cudaMemcpy2DAsync((char*)c + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es, (size_t)ldc * P.es,
-                                        ct, (size_t)ldct * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDeviceToHost,
+                                        ct, (size_t)ldct * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDefault,
                                         ctx->d2h));
         TMM_CUDA(ctx, cudaEventRecord(cs->done, ctx->d2h));
         cs->used = true;
@@ -809,6 +823,40 @@ int sync_all(tmm_context* ctx) {
 
 }  // namespace
 
+// tmm_gemm on device-resident (or managed) operands: the device entry on the first context
+// stream, then a sync.  copy_c_back == false keeps its meaning: the result goes to the
+// compact full-C buffer (beta * C read from c) and c is not written.
+static int gemm_resident(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k, const void* alpha,
+                  const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c,
+                  bool copy_back, std::chrono::steady_clock::time_point t0) {
+  cudaStream_t s = ctx->streams[0];
+  void* dst = c;
+  int64_t ld_dst = ld_c;
+  const size_t es = elem_size(ctx->dtype);
+  if (!copy_back) {
+    TMM_CUDA(ctx, ctx->full_c.reserve((size_t)m * (size_t)n * es));
+    ctx->full_c_elems = (size_t)m * (size_t)n;
+    if (!is_zero(ctx->dtype, beta))
+      TMM_CUDA(ctx, cudaMemcpy2DAsync(ctx->full_c.ptr, (size_t)m * es, c, (size_t)ld_c * es, (size_t)m * es, (size_t)n,
+                                      cudaMemcpyDefault, s));
+    dst = ctx->full_c.ptr;
+    ld_dst = m;
+  }
+  int st = tmm_gemm_device(ctx, trans_a, trans_b, m, n, k, alpha, a, ld_a, b, ld_b, beta, dst, ld_dst, s);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (!st && e != cudaSuccess) st = cuda_fail(ctx, e, "cudaStreamSynchronize");
+  if (!st && ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE) st = check_oz_error(ctx);
+  ctx->stats.tile_m = (int)std::min<int64_t>(m, INT32_MAX);
+  ctx->stats.tile_n = (int)std::min<int64_t>(n, INT32_MAX);
+  ctx->stats.tile_k = (int)std::min<int64_t>(std::max<int64_t>(k, 1), ctx->max_tile_k);
+  ctx->stats.n_streams = 1;
+  ctx->stats.path = (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE) ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
+  ctx->stats.ozaki_slices = ctx->stats.path == TMM_PATH_OZAKI
+                                ? (ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES) : 0;
+  ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
 extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
                         const void* alpha, const void* a, int64_t ld_a, const void* b, int64_t ld_b,
                         const void* beta, void* c, int64_t ld_c, int pin_host_buffers, int copy_c_back) {
@@ -832,6 +880,12 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: null matrix pointer");
   const bool ozaki = ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE;
   DeviceGuard dg(ctx->device);
+
+  // ---- every operand already device-accessible: no host link, no pinning, no tiling of m, n
+  const bool c_used = copy_c_back || beta_nz;
+  if ((k == 0 || (device_accessible(a) && device_accessible(b))) && (!c_used || device_accessible(c)))
+    return gemm_resident(ctx, trans_a, trans_b, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, copy_c_back != 0,
+                         t0);
 
   // ---- tile sizes (src/Tiled-MM/tiled_mm.cpp:557-560)
   int tm, tn, tk;
