@@ -62,6 +62,11 @@ WORKLOADS = {
                       desc="Out-of-core Ozaki FP64 GEMM m=n=32768, k=65536, NT, alpha=-1, beta=1, N(0,1) x row "
                            "factors 2^U[-10,10], pageable host buffers registered per call, copy_c_back=false, "
                            "autotuned tiles and streams"),
+    "sweep": dict(m=20000, n=20000, k=20000, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
+                  path="sweep", tiles=(5000, 5000, 5000), streams=2,
+                  desc="host-pointer FP64 GEMM sweep m=n=k in 4000..20000 step 2000, NN, uniform[-1,1), "
+                       "tiles 5000, 2 streams, pinned: the tiled call, the cublasXt-style entry, the vendor "
+                       "cublasXt and the Ozaki path"),
     "batched512": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
                        path="batched", tiles=(4096, 4096, 4096), streams=2,
                        desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
@@ -474,6 +479,88 @@ def run_batched(args, rank, world, dist, log) -> dict:
                          "peak_source": "measured DMMA issue rate on this pool's GB300"}}
 
 
+def _vendor_cublasxt():
+    """The vendor's cublasXt (comparison only; the library never links cuBLAS)."""
+    import ctypes as C
+
+    for name in ("libcublas.so", "libcublas.so.13", "/usr/local/cuda/lib64/libcublas.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            pass
+    return None
+
+
+def run_sweep(args, rank, world, dist, log) -> dict:
+    """The reference's compare.sh sweep (examples/compare.sh: m = n = k = 4000..20000, tile 5000,
+    2 streams, Tiled-MM's multiply example beside cublasXt-multiply) on this GPU: per size, one
+    warm-up call and args.steps timed calls, host wall time, pinned host buffers, FP64."""
+    import ctypes as C
+
+    import tiledmm as tmm
+
+    sizes = [int(x) for x in args.sweep_sizes.split(",")]
+    reps = max(1, args.steps)
+    vendor = _vendor_cublasxt()
+    rows = []
+
+    def timed(fn):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps
+
+    for size in sizes:
+        m = n = k = size
+        pa, pb, pc = (tmm.PinnedArray((size * size,)) for _ in range(3))
+        tmm.fill_host(pa.array, m, k, m, 0, 0.0, seed=rank, mat_id=0)
+        tmm.fill_host(pb.array, k, n, k, 0, 0.0, seed=rank, mat_id=1)
+        a, b, c = pa.array, pb.array, pc.array
+        flops = 2.0 * m * n * k
+        row = {"size": size}
+        ctx = tmm.make_context(np.float64, 2, 5000, 5000, 5000)
+        row["tiled_tflops"] = flops / timed(lambda: tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)) / 1e12
+        ours = c.copy()
+        ctx.close()
+        xt = tmm.XtHandle(block_dim=5000)
+        row["xt_entry_tflops"] = flops / timed(lambda: xt.gemm(np.float64, 0, 0, m, n, k, 1.0, a, m, b, k, 0.0, c,
+                                                               m)) / 1e12
+        xt.set_path(tmm.PATH_OZAKI, 11)
+        row["xt_entry_ozaki11_tflops"] = flops / timed(lambda: xt.gemm(np.float64, 0, 0, m, n, k, 1.0, a, m, b, k,
+                                                                       0.0, c, m)) / 1e12
+        xt.close()
+        if vendor is not None:
+            h = C.c_void_p()
+            if vendor.cublasXtCreate(C.byref(h)) == 0:
+                devs = (C.c_int * 1)(0)
+                vendor.cublasXtDeviceSelect(h, 1, devs)
+                vendor.cublasXtSetBlockDim(h, 5000)
+                al, be = C.c_double(1.0), C.c_double(0.0)
+                sz = C.c_size_t
+
+                def vendor_call():
+                    st = vendor.cublasXtDgemm(h, 0, 0, sz(m), sz(n), sz(k), C.byref(al), C.c_void_p(a.ctypes.data),
+                                              sz(m), C.c_void_p(b.ctypes.data), sz(k), C.byref(be),
+                                              C.c_void_p(c.ctypes.data), sz(m))
+                    if st != 0:
+                        raise RuntimeError(f"cublasXtDgemm status {st}")
+
+                row["cublasxt_tflops"] = flops / timed(vendor_call) / 1e12
+                row["max_rel_diff_vs_cublasxt"] = float(np.abs(ours - c).max() / max(np.abs(c).max(), 1e-300))
+                vendor.cublasXtDestroy(h)
+        log(json.dumps(row))
+        rows.append(row)
+        for p in (pa, pb, pc):
+            p.free()
+    last = rows[-1]
+    return {"value": last["tiled_tflops"], "ms_per_step": 2.0 * last["size"] ** 3 / last["tiled_tflops"] / 1e9,
+            "sweep": rows, "reps": reps, "warmup": 1,
+            "e2e": {"value": last["tiled_tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 16 * last["size"] ** 2,
+                    "d2h_bytes_per_step": 8 * last["size"] ** 2, "note": "every call is host to host"},
+            "vendor_cublasxt": vendor is not None}
+
+
 def cpu_baseline(w, seconds_budget: float = 20.0) -> dict:
     """The reference algorithm's CPU restatement (the oracle: tiled GEMM with the reference's tile
     semantics, per-tile plain GEMM) on a k-slab of the workload, all host threads."""
@@ -520,6 +607,7 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--tiles", default="", help="tile_m,tile_n,tile_k of the context (overrides the workload's)")
+    ap.add_argument("--sweep-sizes", default="4000,6000,8000,10000,12000,14000,16000,18000,20000")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload], engine=args.engine)
     if args.tiles:
@@ -546,6 +634,16 @@ def main() -> None:
         print(json.dumps(line), flush=True)
         return
 
+    if w["path"] == "sweep":
+        res = run_sweep(args, rank, world, dist, log)
+        if rank == 0:
+            line = dict(base)
+            line["metric"] = "FP64 TFLOP/s of the host-pointer tiled GEMM at the largest sweep size"
+            line.update(res)
+            print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if w["path"] == "batched":
         res = run_batched(args, rank, world, dist, log)
         if rank == 0:

@@ -265,6 +265,33 @@ int tmm_error_metric_f64(char trans_a, char trans_b, int64_t m, int64_t n, int64
                          const double* c0, int64_t ld_c0, const double* c, int64_t ld_c, int64_t n_samples,
                          uint64_t seed, int n_threads, double* metric);
 
+/* ------------------------------------------------------------------ cublasXt-style entry
+ * The call shape of the reference's comparison program against cublasXt
+ * (examples/cublasXt-multiply.cpp:153-167: cublasXtCreate, cublasXtDeviceSelect,
+ * cublasXtSetBlockDim, cublasXt?gemm on host pointers), on the tiled path of this library:
+ * one block dimension for all three tile sizes (default 4096), trans arguments as
+ * cublasOperation_t values (0 = N, 1 = T, 2 = C), host or device pointers, page-locking
+ * for the call and C copied back, synchronous.  The current device is used.
+ * tmm_xt_set_path selects the Ozaki path for tmm_xt_dgemm (slices <= 0: default). */
+typedef struct tmm_xt tmm_xt;
+int tmm_xt_create(tmm_xt** handle);
+int tmm_xt_destroy(tmm_xt* handle);
+int tmm_xt_set_block_dim(tmm_xt* handle, int block_dim);
+int tmm_xt_get_block_dim(tmm_xt* handle, int* block_dim);
+int tmm_xt_set_path(tmm_xt* handle, int path, int ozaki_slices);
+const char* tmm_xt_last_error(tmm_xt* handle);
+int tmm_xt_sgemm(tmm_xt* handle, int transa, int transb, int64_t m, int64_t n, int64_t k, const float* alpha,
+                 const float* a, int64_t ld_a, const float* b, int64_t ld_b, const float* beta, float* c,
+                 int64_t ld_c);
+int tmm_xt_dgemm(tmm_xt* handle, int transa, int transb, int64_t m, int64_t n, int64_t k, const double* alpha,
+                 const double* a, int64_t ld_a, const double* b, int64_t ld_b, const double* beta, double* c,
+                 int64_t ld_c);
+/* complex float / complex double: interleaved (re, im) pairs, as std::complex */
+int tmm_xt_cgemm(tmm_xt* handle, int transa, int transb, int64_t m, int64_t n, int64_t k, const void* alpha,
+                 const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c);
+int tmm_xt_zgemm(tmm_xt* handle, int transa, int transb, int64_t m, int64_t n, int64_t k, const void* alpha,
+                 const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c);
+
 #ifdef __cplusplus
 }
 #endif

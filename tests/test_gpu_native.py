@@ -282,6 +282,36 @@ def test_mixed_host_and_device_operands(tmm):
     np.testing.assert_array_equal(mixed, host)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.complex64, np.complex128])
+@pytest.mark.parametrize("ops", [(0, 0), (1, 2), (2, 1)])
+def test_xt_entry_matches_fixed_tile_call(tmm, dtype, ops):
+    """tmm_xt_?gemm (cublasXt call shape; trans as cublasOperation_t 0/1/2) equals tmm_gemm on
+    a context with fixed tiles of the block dimension, bit for bit; changing the block
+    dimension changes the tiles, not the product beyond rounding."""
+    rng = np.random.default_rng(41)
+    m, n, k = 260, 190, 230
+    ta, tb = ("N", "T", "C")[ops[0]], ("N", "T", "C")[ops[1]]
+    if np.dtype(dtype).kind != "c":
+        ta, tb = ta.replace("C", "T"), tb.replace("C", "T")
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype=dtype, pad=2)
+    xt = tmm.XtHandle(block_dim=96)
+    assert xt.block_dim() == 96
+    got = c.copy()
+    xt.gemm(dtype, ops[0], ops[1], m, n, k, 0.5, a, lda, b, ldb, 1.5, got, ldc)
+    ctx = tmm.make_context(dtype, 2, 96, 96, 96)
+    ctx.set_tile_policy(tmm.TILE_POLICY_FIXED)
+    want = run(tmm, ctx, ta, tb, m, n, k, 0.5, a, lda, b, ldb, 1.5, c.copy(), ldc)
+    np.testing.assert_array_equal(got, want)
+    xt.set_block_dim(4096)
+    other = c.copy()
+    xt.gemm(dtype, ops[0], ops[1], m, n, k, 0.5, a, lda, b, ldb, 1.5, other, ldc)
+    tol = tol_for(dtype, k)
+    np.testing.assert_allclose(other, want, rtol=tol, atol=tol * np.abs(want).max())
+    with pytest.raises(RuntimeError):
+        xt.gemm(dtype, 7, 0, m, n, k, 0.5, a, lda, b, ldb, 1.5, other, ldc)
+    xt.close()
+
+
 def test_device_generator_matches_host(tmm):
     torch = pytest.importorskip("torch")
     rows, cols, ld = 257, 33, 300

@@ -137,7 +137,13 @@ TileChoice autotune_tiles(int dtype, bool ozaki, int slices, int64_t m, int64_t 
   // The Ozaki path amortises its split and its FP64 drains over long k tiles, but past
   // 16384 the slice planes that one wave of CTAs streams outgrow L2: measured at
   // m = n = k = 32768, 11 slices: tk 8192 -> 46.1, 16384 -> 46.9, 32768 -> 43.2 TFLOP/s.
-  int64_t tk = std::min<int64_t>({k > 0 ? k : 1, (int64_t)max_tk, ozaki ? 16384 : 8192});
+  // TMM_AUTOTUNE_OZAKI_TK overrides the cap.
+  int64_t oz_cap = 16384;
+  if (const char* env = getenv("TMM_AUTOTUNE_OZAKI_TK")) {
+    const long long v = atoll(env);
+    if (v >= 128) oz_cap = v;
+  }
+  int64_t tk = std::min<int64_t>({k > 0 ? k : 1, (int64_t)max_tk, ozaki ? oz_cap : 8192});
   int64_t tm = std::min<int64_t>({m, (int64_t)max_tm, 16384});
   int64_t tn = std::min<int64_t>({n, (int64_t)max_tn, 16384});
   auto working_set = [&](int64_t a, int64_t b, int64_t c) -> double {

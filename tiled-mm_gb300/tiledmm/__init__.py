@@ -58,6 +58,16 @@ SIGNATURES = {
     "tmm_ozaki_gemm_device_noalloc": (_ci, [C.c_char, C.c_char, _i64, _i64, _i64, C.c_double, _p, _i64, _p, _i64,
                                             C.c_double, _p, _i64, _ci, _i64, _p]),
     "tmm_gemm_batched": (_ci, [_p, _ci, _p, _ci]),
+    "tmm_xt_create": (_ci, [C.POINTER(_p)]),
+    "tmm_xt_destroy": (_ci, [_p]),
+    "tmm_xt_set_block_dim": (_ci, [_p, _ci]),
+    "tmm_xt_get_block_dim": (_ci, [_p, C.POINTER(_ci)]),
+    "tmm_xt_set_path": (_ci, [_p, _ci, _ci]),
+    "tmm_xt_last_error": (C.c_char_p, [_p]),
+    "tmm_xt_sgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
+    "tmm_xt_dgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
+    "tmm_xt_cgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
+    "tmm_xt_zgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
     "tmm_get_full_c": (_ci, [_p, C.POINTER(_p), C.POINTER(_sz), C.POINTER(_sz)]),
     "tmm_set_num_streams": (_ci, [_p, _ci]),
     "tmm_get_num_streams": (_ci, [_p, C.POINTER(_ci)]),
@@ -307,6 +317,57 @@ class BatchProblem(C.Structure):
     _fields_ = [("dtype", _ci), ("trans_a", C.c_char), ("trans_b", C.c_char), ("m", _i64), ("n", _i64), ("k", _i64),
                 ("alpha", C.c_double), ("beta", C.c_double), ("a", _p), ("ld_a", _i64), ("b", _p), ("ld_b", _i64),
                 ("c", _p), ("ld_c", _i64)]
+
+
+class XtHandle:
+    """cublasXt-style handle (include/tmm_c_api.h, tmm_xt_*): one block dimension for all tile
+    sizes, ?gemm with trans as cublasOperation_t values (0 N, 1 T, 2 C) on host or device
+    pointers, page-locking for the call, synchronous."""
+
+    _FN = {np.float32: "tmm_xt_sgemm", np.float64: "tmm_xt_dgemm", np.complex64: "tmm_xt_cgemm",
+           np.complex128: "tmm_xt_zgemm"}
+    _DT = {np.float32: FLOAT, np.float64: DOUBLE, np.complex64: COMPLEX_FLOAT, np.complex128: COMPLEX_DOUBLE}
+
+    def __init__(self, block_dim: int | None = None):
+        self._h = _p()
+        _check(_lib.tmm_xt_create(C.byref(self._h)))
+        if block_dim is not None:
+            self.set_block_dim(block_dim)
+
+    def _check(self, status: int) -> None:
+        if status != 0:
+            msg = _lib.tmm_xt_last_error(self._h).decode(errors="replace")
+            raise RuntimeError(f"GPU ERROR: {STATUS.get(status, status)}: {msg}")
+
+    def set_block_dim(self, block_dim: int) -> None:
+        self._check(_lib.tmm_xt_set_block_dim(self._h, block_dim))
+
+    def block_dim(self) -> int:
+        v = _ci()
+        self._check(_lib.tmm_xt_get_block_dim(self._h, C.byref(v)))
+        return v.value
+
+    def set_path(self, path: int, slices: int = 0) -> None:
+        self._check(_lib.tmm_xt_set_path(self._h, path, slices))
+
+    def gemm(self, dtype, transa: int, transb: int, m: int, n: int, k: int, alpha, a, lda: int, b, ldb: int, beta,
+             c, ldc: int) -> None:
+        dt = np.dtype(dtype).type
+        al, be = _scalar(self._DT[dt], alpha), _scalar(self._DT[dt], beta)
+        fn = getattr(_lib, self._FN[dt])
+        self._check(fn(self._h, transa, transb, m, n, k, al.ctypes.data, _ptr(a), lda, _ptr(b), ldb, be.ctypes.data,
+                       _ptr(c), ldc))
+
+    def close(self) -> None:
+        if self._h:
+            _lib.tmm_xt_destroy(self._h)
+            self._h = _p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def gemm_batched(ctx: MMHandle, problems: list[dict], device_operands: bool = False) -> None:
