@@ -67,6 +67,10 @@ WORKLOADS = {
                   desc="host-pointer FP64 GEMM sweep m=n=k in 4000..20000 step 2000, NN, uniform[-1,1), "
                        "tiles 5000, 2 streams, pinned: the tiled call, the cublasXt-style entry, the vendor "
                        "cublasXt and the Ozaki path"),
+    "zgemm8192": dict(m=8192, n=8192, k=8192, ta="N", tb="C", alpha=1.0, beta=0.0, kind=0, param=0.0,
+                      path="complex", tiles=(8192, 8192, 8192), streams=2,
+                      desc="complex double GEMM m=n=k=8192, op(B) conjugate-transposed, uniform[-1,1) parts, "
+                           "device-resident: Ozaki path (real embedding) vs the native complex kernel"),
     "batched512": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
                        path="batched", tiles=(4096, 4096, 4096), streams=2,
                        desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
@@ -561,6 +565,54 @@ def run_sweep(args, rank, world, dist, log) -> dict:
             "vendor_cublasxt": vendor is not None}
 
 
+def run_complex(args, w, rank, world, dist, log) -> dict:
+    """Complex double on the device: the Ozaki path (real embedding, tcgen05 engine) against the
+    native complex kernel (FP64 FMA), complex TFLOP/s = 8mnk / time, CUDA events; agreement of
+    the two results on every entry relative to the largest magnitude."""
+    import torch
+
+    import tiledmm as tmm
+
+    m, n, k = w["m"], w["n"], w["k"]
+    g = torch.Generator(device="cuda").manual_seed(rank)
+    a = torch.complex(torch.rand(m * k, dtype=torch.float64, device="cuda", generator=g) * 2 - 1,
+                      torch.rand(m * k, dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
+    b = torch.complex(torch.rand(k * n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1,
+                      torch.rand(k * n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1)
+    slices = args.slices or 11
+    flops = 8.0 * m * n * k
+    out = {}
+    results = {}
+    for name in ("ozaki", "native"):
+        ctx = tmm.make_context(np.complex128, w["streams"], *w["tiles"])
+        if name == "ozaki":
+            ctx.set_path(tmm.PATH_OZAKI, slices)
+            ctx.set_ozaki_engine(w["engine"])
+        c = torch.zeros(m * n, dtype=torch.complex128, device="cuda")
+        stream = torch.cuda.current_stream()
+        call = lambda: tmm.gemm_device(ctx, w["ta"], w["tb"], m, n, k, 1.0, a, m, b, n, 0.0, c, m,
+                                       stream=stream.cuda_stream)
+        for _ in range(args.warmup if name == "ozaki" else 1):
+            call()
+        torch.cuda.synchronize()
+        reps = args.steps if name == "ozaki" else 1
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / reps / 1e3
+        out[name] = {"tflops": flops / t / 1e12, "ms": t * 1e3}
+        results[name] = c
+        ctx.close()
+    diff = (results["ozaki"] - results["native"]).abs().max().item()
+    out["max_abs_diff_over_max_abs"] = diff / results["native"].abs().max().item()
+    out["slices"] = slices
+    return {"value": out["ozaki"]["tflops"], "ms_per_step": out["ozaki"]["ms"], "complex": out,
+            "e2e": None, "gpu_launches": None}
+
+
 def cpu_baseline(w, seconds_budget: float = 20.0) -> dict:
     """The reference algorithm's CPU restatement (the oracle: tiled GEMM with the reference's tile
     semantics, per-tile plain GEMM) on a k-slab of the workload, all host threads."""
@@ -634,6 +686,17 @@ def main() -> None:
         print(json.dumps(line), flush=True)
         return
 
+    if w["path"] == "complex":
+        res = run_complex(args, w, rank, world, dist, log)
+        if rank == 0:
+            line = dict(base)
+            line["metric"] = "complex FP64 TFLOP/s (8mnk / time), Ozaki path vs native complex kernel"
+            line["dtype"] = "c128"
+            line.update(res)
+            print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if w["path"] == "sweep":
         res = run_sweep(args, rank, world, dist, log)
         if rank == 0:

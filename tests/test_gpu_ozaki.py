@@ -184,6 +184,102 @@ def test_device_operands_through_tmm_gemm_ozaki(tmm, oracle):
     np.testing.assert_array_equal(dc.cpu().numpy(), want)
 
 
+# ---------------------------------------------------------------- complex double on the engine
+def _cplx_op(x, ld, t, rows, cols):
+    """op(X) (rows x cols) of a stored column-major complex array."""
+    if t == "N":
+        return x.reshape(-1, ld).T[:rows, :cols]
+    m = x.reshape(-1, ld).T[:cols, :rows].T
+    return m.conj() if t == "C" else m
+
+
+def complex_ozaki_expected(oracle, ta, tb, m, n, k, a, lda, b, ldb, beta, c, ldc, slices, tk, eng):
+    """alpha = 1, real beta: per k tile of tk, the real Ozaki oracle on the embedding
+    [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B], then C = T + beta C (first k tile) or
+    T + C, each operation rounded once as on the GPU."""
+    A, B = _cplx_op(a, lda, ta, m, k), _cplx_op(b, ldb, tb, k, n)
+    C = c.reshape(-1, ldc).T[:m, :n].copy()
+    for kt, k0 in enumerate(range(0, k, tk)):
+        kk = min(tk, k - k0)
+        Ak, Bk = A[:, k0:k0 + kk], B[k0:k0 + kk, :]
+        ahat = np.block([[Ak.real, -Ak.imag], [Ak.imag, Ak.real]])
+        bhat = np.vstack([Bk.real, Bk.imag])
+        t = np.zeros(2 * m * n)
+        ozaki_oracle(oracle, "N", "N", 2 * m, n, 2 * kk, 1.0, ahat.flatten(order="F"), 2 * m,
+                     bhat.flatten(order="F"), 2 * kk, 0.0, t, 2 * m, slices, 2 * kk, eng["k_block"],
+                     eng["pass_blocks"])
+        T = t.reshape(n, 2 * m).T
+        tc = T[:m] + 1j * T[m:]
+        if kt == 0:
+            C = tc + beta * C if beta != 0.0 else tc
+        else:
+            C = tc + C
+    out = c.copy().reshape(-1, ldc).T
+    out[:m, :n] = C
+    return out.T.flatten()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("trans", ["NN", "NT", "TN", "CN", "NC", "CC"])
+def test_complex_ozaki_bit_exact_vs_oracle(tmm, oracle, engine, trans):
+    """Complex double through tmm_gemm on the Ozaki path (tiles 128 x 96 x 80: several C tiles
+    and k tiles, conjugate transposes) equals the oracle's real Ozaki product of the same
+    embedding, combined with the same roundings."""
+    ta, tb = trans
+    rng = np.random.default_rng(ord(ta) * 7 + ord(tb))
+    m, n, k = 230, 170, 200
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype=np.complex128, pad=2)
+    ctx = tmm.make_context(np.complex128, 2, 128, 96, 80)
+    ctx.set_tile_policy(tmm.TILE_POLICY_FIXED)
+    ctx.set_path(tmm.PATH_OZAKI, 7)
+    ctx.set_ozaki_engine(engine)
+    out = c.copy()
+    tmm.gemm(ctx, ta, tb, m, n, k, 1.0, a, lda, b, ldb, 0.5, out, ldc)
+    want = complex_ozaki_expected(oracle, ta, tb, m, n, k, a, lda, b, ldb, 0.5, c, ldc, 7, 80, ctx.ozaki_engine())
+    np.testing.assert_array_equal(out, want)
+    assert ctx.stats()["path"] == tmm.PATH_OZAKI
+
+
+def test_complex_ozaki_gaussian_integers_exact(tmm):
+    """Gaussian integers with small parts are one exact digit per part: the product is exact."""
+    rng = np.random.default_rng(5)
+    m, n, k = 150, 120, 333
+    a = (rng.integers(-9, 10, m * k) + 1j * rng.integers(-9, 10, m * k)).astype(np.complex128)
+    b = (rng.integers(-9, 10, k * n) + 1j * rng.integers(-9, 10, k * n)).astype(np.complex128)
+    c = (rng.integers(-9, 10, m * n) + 1j * rng.integers(-9, 10, m * n)).astype(np.complex128)
+    ctx = tmm.make_context(np.complex128, 2, 4096, 4096, 4096)
+    ctx.set_path(tmm.PATH_OZAKI, 2)
+    out = c.copy()
+    tmm.gemm(ctx, "N", "N", m, n, k, 2 - 1j, a, m, b, k, 1j, out, m)
+    want = (2 - 1j) * (a.reshape(k, m).T @ b.reshape(n, k).T) + 1j * c.reshape(n, m).T
+    np.testing.assert_array_equal(out.reshape(n, m).T, want)
+
+
+def test_complex_ozaki_device_entry_and_accuracy(tmm):
+    """Device entry equals the host entry bit for bit (one k tile each), and with 13 slices the
+    result agrees with the double-precision complex product to a few ulps of its magnitude,
+    for complex alpha and beta."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(6)
+    m, n, k = 300, 260, 400
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "C", m, n, k, dtype=np.complex128, pad=1)
+    ctx = tmm.make_context(np.complex128, 2, 4096, 4096, 4096)
+    ctx.set_path(tmm.PATH_OZAKI, 13)
+    alpha, beta = 0.75 - 0.25j, -0.5 + 1j
+    host = c.copy()
+    tmm.gemm(ctx, "T", "C", m, n, k, alpha, a, lda, b, ldb, beta, host, ldc)
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    s = torch.cuda.current_stream()
+    tmm.gemm_device(ctx, "T", "C", m, n, k, alpha, da, lda, db, ldb, beta, dc, ldc, stream=s.cuda_stream)
+    s.synchronize()
+    np.testing.assert_array_equal(dc.cpu().numpy(), host)
+    A, B = _cplx_op(a, lda, "T", m, k), _cplx_op(b, ldb, "C", k, n)
+    want = alpha * (A @ B) + beta * c.reshape(-1, ldc).T[:m, :n]
+    got = host.reshape(-1, ldc).T[:m, :n]
+    scale = np.abs(A).max() * np.abs(B).max() * k
+    assert np.abs(got - want).max() <= 1e-14 * scale
+
+
 def test_ozaki_needs_double(tmm):
     ctx = tmm.make_context(np.float32, 2, 64, 64, 64)
     with pytest.raises(RuntimeError, match="GPU ERROR"):

@@ -101,6 +101,9 @@ struct tmm_context {
 
   // optional timing of the engine kernels (tmm_set_kernel_timing): event pairs recorded
   // on the launching stream around each launch, summed by tmm_get_kernel_time
+  // complex double on the Ozaki engine: embedding, digit planes and real product, per stream slot
+  std::vector<tmm::GrowBuffer> cz_scratch;
+
   bool ktime = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_pending, kt_free;
   double kt_seconds = 0.0;

@@ -411,8 +411,9 @@ extern "C" int tmm_set_path(tmm_context* ctx, int path, int slices) {
   if (!ctx) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: null context");
   if (path != TMM_PATH_NATIVE && path != TMM_PATH_OZAKI)
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: unknown path");
-  if (path == TMM_PATH_OZAKI && ctx->dtype != TMM_DOUBLE)
-    return fail(ctx, TMM_ERROR_NOT_SUPPORTED, "tmm_set_path: the Ozaki path emulates FP64 and needs a double context");
+  if (path == TMM_PATH_OZAKI && ctx->dtype != TMM_DOUBLE && ctx->dtype != TMM_COMPLEX_DOUBLE)
+    return fail(ctx, TMM_ERROR_NOT_SUPPORTED,
+                "tmm_set_path: the Ozaki path emulates FP64 and needs a double or complex double context");
   if (slices > tmm::OZ_MAX_SLICES)
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: too many slices");
   ctx->path = path;
@@ -537,6 +538,66 @@ double* oz_workspace(tmm_context* ctx, int stream_index) {
 }
 int* oz_error_word(tmm_context* ctx) { return ctx->oz_work.ptr ? (int*)ctx->oz_work.ptr : nullptr; }
 // after synchronisation: a bounded device wait that gave up
+int check_oz_error(tmm_context* ctx);
+
+// Complex double on the Ozaki engine (the reference multiplies complex tiles with
+// cublasZgemm, src/Tiled-MM/tiled_mm.cpp:247-268): per k tile of at most max_tile_k, the
+// real embedding of op(A) and op(B) (tmm_ozaki_complex.cu) is split and multiplied by the
+// real engine into T = [Re; Im], then combined into C with the complex alpha and beta
+// (beta on the first k tile only).  Scratch of stream slot `slot`; the caller has reserved
+// the engine's workspace (reserve_oz_work) for that slot.
+int complex_ozaki(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
+                  const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c,
+                  cudaStream_t s, int slot) {
+  if (m <= 0 || n <= 0) return TMM_SUCCESS;
+  const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+  const int64_t tk = std::max<int64_t>(1, std::min<int64_t>(k, ctx->max_tile_k));
+  const int64_t m2 = 2 * m, k2 = 2 * tk;
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t ahat = up((size_t)m2 * (size_t)k2 * 8), bhat = up((size_t)k2 * (size_t)n * 8);
+  const size_t tbuf = up((size_t)m2 * (size_t)n * 8);
+  const size_t sa = up(tmm::ozaki_split_bytes(m2, k2, slices)), sb = up(tmm::ozaki_split_bytes(n, k2, slices));
+  if ((int)ctx->cz_scratch.size() <= slot) ctx->cz_scratch.resize((size_t)slot + 1);
+  tmm::GrowBuffer& buf = ctx->cz_scratch[(size_t)slot];
+  TMM_CUDA(ctx, buf.reserve(ahat + bhat + tbuf + sa + sb));
+  char* base = (char*)buf.ptr;
+  double* Ahat = (double*)base;
+  double* Bhat = (double*)(base + ahat);
+  double* T = (double*)(base + ahat + bhat);
+  char* SA = base + ahat + bhat + tbuf;
+  char* SB = SA + sa;
+  const double one[2] = {1.0, 0.0};
+  constexpr size_t es = 16;
+  if (k == 0) {  // C = beta * C
+    TMM_CUDA(ctx, cudaMemsetAsync(T, 0, (size_t)m2 * (size_t)n * 8, s));
+    TMM_CUDA(ctx, tmm::ozaki_complex_combine(m, n, (const double*)alpha, (const double*)beta, true, T, c, ld_c, s));
+    return TMM_SUCCESS;
+  }
+  for (int64_t k0 = 0, kt = 0; k0 < k; k0 += tk, ++kt) {
+    const int64_t kk = std::min(tk, k - k0);
+    const char* ab = (const char*)a + (size_t)(opa == tmm::OP_N ? k0 * ld_a : k0) * es;
+    const char* bb = (const char*)b + (size_t)(opb == tmm::OP_N ? k0 : k0 * ld_b) * es;
+    tmm::OzakiSplit va = tmm::ozaki_split_view(SA, m2, 2 * kk, slices, ctx->oz_engine);
+    tmm::OzakiSplit vb = tmm::ozaki_split_view(SB, n, 2 * kk, slices, ctx->oz_engine);
+    // Ahat: 2m x 2kk, ld 2m; Bhat: 2kk x n, ld 2kk (lines of the split: rows of Ahat, columns of Bhat)
+    cudaError_t e = tmm::ozaki_complex_embed(ab, ld_a, opa, bb, ld_b, opb, m, n, kk, Ahat, Bhat, s);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Ahat, m2, tmm::OP_N, m2, 2 * kk, va, s);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Bhat, 2 * kk, tmm::OP_T, n, 2 * kk, vb, s);
+    if (e == cudaSuccess) {
+      KernelTimer timer(ctx, s);
+      e = tmm::ozaki_gemm(va, vb, m2, n, 1.0, 0.0, true, T, m2, ctx->oz_engine, oz_workspace(ctx, slot),
+                          oz_error_word(ctx), s);
+      timer.done();
+    }
+    if (e == cudaSuccess)
+      e = tmm::ozaki_complex_combine(m, n, (const double*)alpha, kt == 0 ? (const double*)beta : one, true, T, c,
+                                     ld_c, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "complex ozaki launch");
+    ctx->stats.kernels += 8;  // two embeddings, two two-kernel splits, the product, the combine
+  }
+  return TMM_SUCCESS;
+}
+
 int check_oz_error(tmm_context* ctx) {
   if (!ctx->oz_work.ptr || ctx->oz_engine != tmm::OZ_ENGINE_TCGEN05) return TMM_SUCCESS;
   int word = 0;
@@ -555,6 +616,7 @@ struct Plan {
   Op opa, opb;
   size_t es;
   bool ozaki;
+  bool cz;  // complex double on the Ozaki engine: raw tiles, per-tile real embedding
   int slices;
   size_t a_slot_bytes, b_slot_bytes, c_slot_bytes, staging_bytes;
 };
@@ -686,6 +748,10 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
     st = setup_cache(ctx, ctx->cache_b, ctx->pool_b, n_b, P.b_slot_bytes);
     if (st) return st;
   }
+  if (P.cz) {
+    st = reserve_oz_work(ctx, ns);
+    if (st) return st;
+  }
   if (P.ozaki) {
     st = reserve_oz_work(ctx, ns);
     if (st) return st;
@@ -776,7 +842,9 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         if (!P.ozaki) {
           const int64_t lda_t = P.opa == tmm::OP_N ? mi : kk;
           const int64_t ldb_t = P.opb == tmm::OP_N ? kk : nj;
-          st = launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s);
+          st = P.cz ? complex_ozaki(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s,
+                                    sidx)
+                    : launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s);
           if (st) return st;
         } else {
           tmm::OzakiSplit va = tmm::ozaki_split_view(SA.ptr, mi, kk, P.slices, P.engine);
@@ -845,7 +913,7 @@ static int gemm_resident(tmm_context* ctx, char trans_a, char trans_b, int64_t m
   int st = tmm_gemm_device(ctx, trans_a, trans_b, m, n, k, alpha, a, ld_a, b, ld_b, beta, dst, ld_dst, s);
   const cudaError_t e = cudaStreamSynchronize(s);
   if (!st && e != cudaSuccess) st = cuda_fail(ctx, e, "cudaStreamSynchronize");
-  if (!st && ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE) st = check_oz_error(ctx);
+  if (!st && ctx->path == TMM_PATH_OZAKI) st = check_oz_error(ctx);
   ctx->stats.tile_m = (int)std::min<int64_t>(m, INT32_MAX);
   ctx->stats.tile_n = (int)std::min<int64_t>(n, INT32_MAX);
   ctx->stats.tile_k = (int)std::min<int64_t>(std::max<int64_t>(k, 1), ctx->max_tile_k);
@@ -920,6 +988,7 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   P.ntm = ntiles(m, tm); P.ntn = ntiles(n, tn); P.ntk = ntiles(k, tk);
   P.es = elem_size(ctx->dtype);
   P.ozaki = ozaki;
+  P.cz = ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_COMPLEX_DOUBLE;
   P.slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
   P.engine = ctx->oz_engine;
   if (ozaki) {
@@ -948,12 +1017,12 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   ctx->stats.tile_n = tn;
   ctx->stats.tile_k = tk;
   ctx->stats.n_streams = (int)std::min<int64_t>(ctx->n_streams, P.ntm * P.ntn);
-  ctx->stats.path = ozaki ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
+  ctx->stats.path = (ozaki || P.cz) ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
   ctx->stats.ozaki_slices = ozaki ? P.slices : 0;
   if (!st) st = run_gemm(ctx, P, alpha, a, ld_a, b, ld_b, beta, c, ld_c, copy_c_back != 0);
   int st2 = sync_all(ctx);  // returns with C final (the reference syncs the device: tiled_mm.cpp:602-604)
   if (!st) st = st2;
-  if (!st && ozaki) st = check_oz_error(ctx);
+  if (!st && (ozaki || P.cz)) st = check_oz_error(ctx);
   unpin(pa);
   unpin(pb);
   unpin(pc);
@@ -1005,6 +1074,11 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
       ctx->stats.kernels += 3;
     }
     return TMM_SUCCESS;
+  }
+  if (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_COMPLEX_DOUBLE) {
+    int st = reserve_oz_work(ctx, 1);
+    if (st) return st;
+    return complex_ozaki(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s, 0);
   }
   return launch_tile_gemm(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s);
 }

@@ -77,6 +77,15 @@ size_t ozaki_workspace_bytes(int engine);
 int64_t ozaki_pass_blocks(int engine);
 int64_t ozaki_k_block(int engine);
 
+// Complex double on the engine (tmm_ozaki_complex.cu): Ahat (2m x 2k, ld 2m) and Bhat
+// (2k x n, ld 2k) are the real embedding of op(A) and op(B) (op C conjugates), whose real
+// product T (2m x n) holds Re C on top of Im C; combine applies the complex alpha and beta'
+// (beta' = beta on the first k-tile, C not read when it is zero; 1 after).
+cudaError_t ozaki_complex_embed(const void* A, int64_t lda, Op opa, const void* B, int64_t ldb, Op opb, int64_t m,
+                                int64_t n, int64_t k, double* Ahat, double* Bhat, cudaStream_t s);
+cudaError_t ozaki_complex_combine(int64_t m, int64_t n, const double* alpha, const double* beta, bool first,
+                                  const double* T, void* C, int64_t ldc, cudaStream_t s);
+
 // sets the message that tmm_last_error(NULL) returns on the calling thread (tmm_core.cpp)
 void set_last_error_message(const char* msg);
 
