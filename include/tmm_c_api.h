@@ -184,8 +184,12 @@ int tmm_get_max_tile_sizes(tmm_context* ctx, int* tile_m, int* tile_n, int* tile
 /* mm_handle::set_streams_and_tiles (src/Tiled-MM/mm_handle.cpp:135-145). */
 int tmm_set_streams_and_tiles(tmm_context* ctx, int n_streams, int tile_m, int tile_n, int tile_k);
 
-/* New: multiplication path for TMM_DOUBLE contexts and the Ozaki slice count
- * (slices <= 0 selects the default). */
+/* New: multiplication path and the Ozaki slice count (slices <= 0 selects the default:
+ * 13 for double and complex double, 6 for float and complex float).  On TMM_PATH_OZAKI,
+ * double contexts split their cached tiles; float, complex float and complex double
+ * contexts cache raw tiles and multiply each tile's real FP64 embedding (complex:
+ * [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B]) on the same engine, alpha and beta applied
+ * in double and the result rounded once to the context's type. */
 int tmm_set_path(tmm_context* ctx, int path, int ozaki_slices);
 int tmm_get_path(tmm_context* ctx, int* path, int* ozaki_slices);
 
@@ -272,7 +276,7 @@ int tmm_error_metric_f64(char trans_a, char trans_b, int64_t m, int64_t n, int64
  * one block dimension for all three tile sizes (default 4096), trans arguments as
  * cublasOperation_t values (0 = N, 1 = T, 2 = C), host or device pointers, page-locking
  * for the call and C copied back, synchronous.  The current device is used.
- * tmm_xt_set_path selects the Ozaki path for tmm_xt_dgemm (slices <= 0: default). */
+ * tmm_xt_set_path selects the path of all four calls (slices <= 0: each type's default). */
 typedef struct tmm_xt tmm_xt;
 int tmm_xt_create(tmm_xt** handle);
 int tmm_xt_destroy(tmm_xt* handle);

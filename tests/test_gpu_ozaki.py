@@ -184,9 +184,11 @@ def test_device_operands_through_tmm_gemm_ozaki(tmm, oracle):
     np.testing.assert_array_equal(dc.cpu().numpy(), want)
 
 
-# ---------------------------------------------------------------- complex double on the engine
+# ------------------------------------------------ float and complex on the engine (real embedding)
 def _cplx_op(x, ld, t, rows, cols):
-    """op(X) (rows x cols) of a stored column-major complex array."""
+    """op(X) (rows x cols) of a stored column-major array, widened to float64 / complex128."""
+    wide = np.complex128 if np.iscomplexobj(x) else np.float64
+    x = x.astype(wide)
     if t == "N":
         return x.reshape(-1, ld).T[:rows, :cols]
     m = x.reshape(-1, ld).T[:cols, :rows].T
@@ -194,26 +196,34 @@ def _cplx_op(x, ld, t, rows, cols):
 
 
 def complex_ozaki_expected(oracle, ta, tb, m, n, k, a, lda, b, ldb, beta, c, ldc, slices, tk, eng):
-    """alpha = 1, real beta: per k tile of tk, the real Ozaki oracle on the embedding
-    [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B], then C = T + beta C (first k tile) or
-    T + C, each operation rounded once as on the GPU."""
+    """alpha = 1, real beta: per k tile of tk, the real Ozaki oracle on the FP64 embedding
+    (float: op(A) x op(B); complex: [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B]), then
+    C = T + beta C (first k tile) or T + C in double, rounded to C's type after every k
+    tile, as on the GPU."""
+    cplx = np.iscomplexobj(c)
     A, B = _cplx_op(a, lda, ta, m, k), _cplx_op(b, ldb, tb, k, n)
     C = c.reshape(-1, ldc).T[:m, :n].copy()
     for kt, k0 in enumerate(range(0, k, tk)):
         kk = min(tk, k - k0)
         Ak, Bk = A[:, k0:k0 + kk], B[k0:k0 + kk, :]
-        ahat = np.block([[Ak.real, -Ak.imag], [Ak.imag, Ak.real]])
-        bhat = np.vstack([Bk.real, Bk.imag])
-        t = np.zeros(2 * m * n)
-        ozaki_oracle(oracle, "N", "N", 2 * m, n, 2 * kk, 1.0, ahat.flatten(order="F"), 2 * m,
-                     bhat.flatten(order="F"), 2 * kk, 0.0, t, 2 * m, slices, 2 * kk, eng["k_block"],
-                     eng["pass_blocks"])
-        T = t.reshape(n, 2 * m).T
-        tc = T[:m] + 1j * T[m:]
-        if kt == 0:
-            C = tc + beta * C if beta != 0.0 else tc
+        if cplx:
+            ahat = np.block([[Ak.real, -Ak.imag], [Ak.imag, Ak.real]])
+            bhat = np.vstack([Bk.real, Bk.imag])
         else:
-            C = tc + C
+            ahat, bhat = Ak, Bk
+        me, ke = ahat.shape
+        t = np.zeros(me * n)
+        ozaki_oracle(oracle, "N", "N", me, n, ke, 1.0, np.asfortranarray(ahat).flatten(order="F"), me,
+                     np.asfortranarray(bhat).flatten(order="F"), ke, 0.0, t, me, slices, ke, eng["k_block"],
+                     eng["pass_blocks"])
+        T = t.reshape(n, me).T
+        tc = T[:m] + 1j * T[m:] if cplx else T
+        Cw = C.astype(np.complex128 if cplx else np.float64)
+        if kt == 0:
+            Cw = tc + beta * Cw if beta != 0.0 else tc
+        else:
+            Cw = tc + Cw
+        C = Cw.astype(c.dtype)
     out = c.copy().reshape(-1, ldc).T
     out[:m, :n] = C
     return out.T.flatten()
@@ -280,7 +290,74 @@ def test_complex_ozaki_device_entry_and_accuracy(tmm):
     assert np.abs(got - want).max() <= 1e-14 * scale
 
 
-def test_ozaki_needs_double(tmm):
-    ctx = tmm.make_context(np.float32, 2, 64, 64, 64)
-    with pytest.raises(RuntimeError, match="GPU ERROR"):
-        ctx.set_path(tmm.PATH_OZAKI, 8)
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("dtype,trans", [(np.float32, "NN"), (np.float32, "NT"), (np.float32, "TN"),
+                                         (np.float32, "TT"), (np.complex64, "NN"), (np.complex64, "CN"),
+                                         (np.complex64, "NC"), (np.complex64, "TC")])
+def test_float_ozaki_bit_exact_vs_oracle(tmm, oracle, engine, dtype, trans):
+    """Float and complex float through tmm_gemm on the Ozaki path (several C tiles and k tiles)
+    equal the oracle's real Ozaki product of the FP64 embedding, combined in double and rounded
+    to the context's type after every k tile."""
+    ta, tb = trans
+    rng = np.random.default_rng(ord(ta) * 11 + ord(tb) + np.dtype(dtype).itemsize)
+    m, n, k = 230, 170, 200
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype=dtype, pad=2)
+    ctx = tmm.make_context(dtype, 2, 128, 96, 80)
+    ctx.set_tile_policy(tmm.TILE_POLICY_FIXED)
+    ctx.set_path(tmm.PATH_OZAKI, 5)
+    ctx.set_ozaki_engine(engine)
+    out = c.copy()
+    tmm.gemm(ctx, ta, tb, m, n, k, 1.0, a, lda, b, ldb, 0.5, out, ldc)
+    want = complex_ozaki_expected(oracle, ta, tb, m, n, k, a, lda, b, ldb, 0.5, c, ldc, 5, 80, ctx.ozaki_engine())
+    np.testing.assert_array_equal(out, want)
+    st = ctx.stats()
+    assert st["path"] == tmm.PATH_OZAKI and st["ozaki_slices"] == 5
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.complex64])
+def test_float_ozaki_default_slices_beat_native(tmm, dtype):
+    """With the float default (6 slices) the Ozaki path's componentwise error is below the
+    native FP32 path's on the same problem and within a few units of FP32 rounding;
+    general alpha and beta; the device entry equals the host entry bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(17)
+    m, n, k = 384, 320, 3000
+    ta, tb = ("T", "N") if dtype == np.float32 else ("C", "N")
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype=dtype, pad=1)
+    alpha, beta = (0.75, -1.25) if dtype == np.float32 else (0.75 - 0.5j, -1.25 + 0.25j)
+    oz = tmm.make_context(dtype, 2, 4096, 4096, 4096)
+    oz.set_path(tmm.PATH_OZAKI, 0)
+    assert oz.get_path() == (tmm.PATH_OZAKI, 6)
+    nat = tmm.make_context(dtype, 2, 4096, 4096, 4096)
+    got_oz, got_nat = c.copy(), c.copy()
+    tmm.gemm(oz, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, got_oz, ldc)
+    tmm.gemm(nat, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, got_nat, ldc)
+    A, B = _cplx_op(a, lda, ta, m, k), _cplx_op(b, ldb, tb, k, n)
+    C0 = _cplx_op(c, ldc, "N", m, n)
+    exact = alpha * (A @ B) + beta * C0
+    den = abs(alpha) * (np.abs(A) @ np.abs(B)) + abs(beta) * np.abs(C0)
+    if dtype == np.complex64:
+        den = 2 * den  # |Re| and |Im| parts each bounded by the sum of the component magnitudes
+    def err(x):
+        return float(np.max(np.abs(_cplx_op(x, ldc, "N", m, n) - exact) / den))
+    e_oz, e_nat = err(got_oz), err(got_nat)
+    assert e_oz <= e_nat
+    assert e_oz <= 4 * 2.0 ** -24
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    s = torch.cuda.current_stream()
+    tmm.gemm_device(oz, ta, tb, m, n, k, alpha, da, lda, db, ldb, beta, dc, ldc, stream=s.cuda_stream)
+    s.synchronize()
+    np.testing.assert_array_equal(dc.cpu().numpy(), got_oz)
+
+
+def test_ozaki_default_slices_per_type(tmm):
+    for dtype, want in ((np.float32, 6), (np.complex64, 6), (np.float64, 13), (np.complex128, 13)):
+        ctx = tmm.make_context(dtype, 2, 64, 64, 64)
+        ctx.set_path(tmm.PATH_OZAKI, 0)
+        assert ctx.get_path() == (tmm.PATH_OZAKI, want)
+        ctx.set_path(tmm.PATH_OZAKI, 9)
+        assert ctx.get_path() == (tmm.PATH_OZAKI, 9)
+    with pytest.raises(RuntimeError):
+        ctx.set_path(tmm.PATH_OZAKI, 99)
+
+

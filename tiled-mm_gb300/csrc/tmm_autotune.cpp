@@ -146,7 +146,18 @@ TileChoice autotune_tiles(int dtype, bool ozaki, int slices, int64_t m, int64_t 
   int64_t tk = std::min<int64_t>({k > 0 ? k : 1, (int64_t)max_tk, ozaki ? oz_cap : 8192});
   int64_t tm = std::min<int64_t>({m, (int64_t)max_tm, 16384});
   int64_t tn = std::min<int64_t>({n, (int64_t)max_tn, 16384});
+  // float and complex contexts on the Ozaki path cache raw tiles and give each of the two
+  // streams the tile's FP64 embedding (twice as tall and deep for complex), its product
+  // and its slices
+  const bool embed = ozaki && dtype != TMM_DOUBLE;
+  const double cf = dtype == TMM_COMPLEX_FLOAT || dtype == TMM_COMPLEX_DOUBLE ? 2.0 : 1.0;
   auto working_set = [&](int64_t a, int64_t b, int64_t c) -> double {
+    if (embed) {
+      const double raw = 2.0 * es * a * c + 2.0 * es * b * c + 4.0 * es * a * b;
+      const double per_stream = 8.0 * cf * cf * a * c + 8.0 * cf * c * b + 8.0 * cf * a * b +
+                                (double)slices * (cf * a + b) * cf * c;
+      return raw + 2.0 * per_stream;
+    }
     // two A tiles, two B tiles (cached form), four C tiles (2 streams x 2 slots), staging
     const double tile_a = ozaki ? (double)slices * a * c : (double)es * a * c;
     const double tile_b = ozaki ? (double)slices * b * c : (double)es * b * c;

@@ -411,13 +411,10 @@ extern "C" int tmm_set_path(tmm_context* ctx, int path, int slices) {
   if (!ctx) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: null context");
   if (path != TMM_PATH_NATIVE && path != TMM_PATH_OZAKI)
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: unknown path");
-  if (path == TMM_PATH_OZAKI && ctx->dtype != TMM_DOUBLE && ctx->dtype != TMM_COMPLEX_DOUBLE)
-    return fail(ctx, TMM_ERROR_NOT_SUPPORTED,
-                "tmm_set_path: the Ozaki path emulates FP64 and needs a double or complex double context");
   if (slices > tmm::OZ_MAX_SLICES)
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_set_path: too many slices");
   ctx->path = path;
-  ctx->ozaki_slices = slices > 0 ? slices : tmm::OZ_DEFAULT_SLICES;
+  ctx->ozaki_slices = slices > 0 ? slices : tmm::oz_default_slices(ctx->dtype);
   return TMM_SUCCESS;
 }
 
@@ -540,23 +537,26 @@ int* oz_error_word(tmm_context* ctx) { return ctx->oz_work.ptr ? (int*)ctx->oz_w
 // after synchronisation: a bounded device wait that gave up
 int check_oz_error(tmm_context* ctx);
 
-// Complex double on the Ozaki engine (the reference multiplies complex tiles with
-// cublasZgemm, src/Tiled-MM/tiled_mm.cpp:247-268): per k tile of at most max_tile_k, the
-// real embedding of op(A) and op(B) (tmm_ozaki_complex.cu) is split and multiplied by the
-// real engine into T = [Re; Im], then combined into C with the complex alpha and beta
-// (beta on the first k tile only).  Scratch of stream slot `slot`; the caller has reserved
-// the engine's workspace (reserve_oz_work) for that slot.
-int complex_ozaki(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
-                  const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c,
-                  cudaStream_t s, int slot) {
+// Float, complex float and complex double on the Ozaki engine (the reference multiplies
+// these tiles with cublasSgemm / cublasCgemm / cublasZgemm, src/Tiled-MM/tiled_mm.cpp:226-268):
+// per k tile of at most max_tile_k, the real FP64 embedding of op(A) and op(B)
+// (tmm_ozaki_embed.cu) is split and multiplied by the real engine into T, then combined
+// into C with alpha and beta (beta on the first k tile only), rounded once to the
+// context's type.  Scratch of stream slot `slot`; the caller has reserved the engine's
+// workspace (reserve_oz_work) for that slot.
+int embedded_ozaki(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
+                   const void* a, int64_t ld_a, const void* b, int64_t ld_b, const void* beta, void* c, int64_t ld_c,
+                   cudaStream_t s, int slot) {
   if (m <= 0 || n <= 0) return TMM_SUCCESS;
-  const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+  const int dt = ctx->dtype;
+  const bool cplx = dt == TMM_COMPLEX_FLOAT || dt == TMM_COMPLEX_DOUBLE;
+  const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::oz_default_slices(dt);
   const int64_t tk = std::max<int64_t>(1, std::min<int64_t>(k, ctx->max_tile_k));
-  const int64_t m2 = 2 * m, k2 = 2 * tk;
+  const int64_t me = cplx ? 2 * m : m, ke = cplx ? 2 * tk : tk;  // embedded sizes
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-  const size_t ahat = up((size_t)m2 * (size_t)k2 * 8), bhat = up((size_t)k2 * (size_t)n * 8);
-  const size_t tbuf = up((size_t)m2 * (size_t)n * 8);
-  const size_t sa = up(tmm::ozaki_split_bytes(m2, k2, slices)), sb = up(tmm::ozaki_split_bytes(n, k2, slices));
+  const size_t ahat = up((size_t)me * (size_t)ke * 8), bhat = up((size_t)ke * (size_t)n * 8);
+  const size_t tbuf = up((size_t)me * (size_t)n * 8);
+  const size_t sa = up(tmm::ozaki_split_bytes(me, ke, slices)), sb = up(tmm::ozaki_split_bytes(n, ke, slices));
   if ((int)ctx->cz_scratch.size() <= slot) ctx->cz_scratch.resize((size_t)slot + 1);
   tmm::GrowBuffer& buf = ctx->cz_scratch[(size_t)slot];
   TMM_CUDA(ctx, buf.reserve(ahat + bhat + tbuf + sa + sb));
@@ -566,33 +566,33 @@ int complex_ozaki(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_
   double* T = (double*)(base + ahat + bhat);
   char* SA = base + ahat + bhat + tbuf;
   char* SB = SA + sa;
-  const double one[2] = {1.0, 0.0};
-  constexpr size_t es = 16;
+  char one[16] = {0};
+  if (dt == TMM_FLOAT || dt == TMM_COMPLEX_FLOAT) *(float*)one = 1.f;
+  else *(double*)one = 1.0;
+  const size_t es = elem_size(dt);
   if (k == 0) {  // C = beta * C
-    TMM_CUDA(ctx, cudaMemsetAsync(T, 0, (size_t)m2 * (size_t)n * 8, s));
-    TMM_CUDA(ctx, tmm::ozaki_complex_combine(m, n, (const double*)alpha, (const double*)beta, true, T, c, ld_c, s));
+    TMM_CUDA(ctx, cudaMemsetAsync(T, 0, (size_t)me * (size_t)n * 8, s));
+    TMM_CUDA(ctx, tmm::ozaki_combine(dt, m, n, alpha, beta, true, T, c, ld_c, s));
     return TMM_SUCCESS;
   }
   for (int64_t k0 = 0, kt = 0; k0 < k; k0 += tk, ++kt) {
-    const int64_t kk = std::min(tk, k - k0);
+    const int64_t kk = std::min(tk, k - k0), kke = cplx ? 2 * kk : kk;
     const char* ab = (const char*)a + (size_t)(opa == tmm::OP_N ? k0 * ld_a : k0) * es;
     const char* bb = (const char*)b + (size_t)(opb == tmm::OP_N ? k0 : k0 * ld_b) * es;
-    tmm::OzakiSplit va = tmm::ozaki_split_view(SA, m2, 2 * kk, slices, ctx->oz_engine);
-    tmm::OzakiSplit vb = tmm::ozaki_split_view(SB, n, 2 * kk, slices, ctx->oz_engine);
-    // Ahat: 2m x 2kk, ld 2m; Bhat: 2kk x n, ld 2kk (lines of the split: rows of Ahat, columns of Bhat)
-    cudaError_t e = tmm::ozaki_complex_embed(ab, ld_a, opa, bb, ld_b, opb, m, n, kk, Ahat, Bhat, s);
-    if (e == cudaSuccess) e = tmm::ozaki_split(Ahat, m2, tmm::OP_N, m2, 2 * kk, va, s);
-    if (e == cudaSuccess) e = tmm::ozaki_split(Bhat, 2 * kk, tmm::OP_T, n, 2 * kk, vb, s);
+    tmm::OzakiSplit va = tmm::ozaki_split_view(SA, me, kke, slices, ctx->oz_engine);
+    tmm::OzakiSplit vb = tmm::ozaki_split_view(SB, n, kke, slices, ctx->oz_engine);
+    // Ahat: me x kke, ld me; Bhat: kke x n, ld kke (lines of the split: rows of Ahat, columns of Bhat)
+    cudaError_t e = tmm::ozaki_embed(dt, ab, ld_a, opa, bb, ld_b, opb, m, n, kk, Ahat, Bhat, s);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Ahat, me, tmm::OP_N, me, kke, va, s);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Bhat, kke, tmm::OP_T, n, kke, vb, s);
     if (e == cudaSuccess) {
       KernelTimer timer(ctx, s);
-      e = tmm::ozaki_gemm(va, vb, m2, n, 1.0, 0.0, true, T, m2, ctx->oz_engine, oz_workspace(ctx, slot),
+      e = tmm::ozaki_gemm(va, vb, me, n, 1.0, 0.0, true, T, me, ctx->oz_engine, oz_workspace(ctx, slot),
                           oz_error_word(ctx), s);
       timer.done();
     }
-    if (e == cudaSuccess)
-      e = tmm::ozaki_complex_combine(m, n, (const double*)alpha, kt == 0 ? (const double*)beta : one, true, T, c,
-                                     ld_c, s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "complex ozaki launch");
+    if (e == cudaSuccess) e = tmm::ozaki_combine(dt, m, n, alpha, kt == 0 ? beta : (const void*)one, true, T, c, ld_c, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "embedded ozaki launch");
     ctx->stats.kernels += 8;  // two embeddings, two two-kernel splits, the product, the combine
   }
   return TMM_SUCCESS;
@@ -616,7 +616,7 @@ struct Plan {
   Op opa, opb;
   size_t es;
   bool ozaki;
-  bool cz;  // complex double on the Ozaki engine: raw tiles, per-tile real embedding
+  bool embed;  // float / complex on the Ozaki engine: raw tiles, per-tile real FP64 embedding
   int slices;
   size_t a_slot_bytes, b_slot_bytes, c_slot_bytes, staging_bytes;
 };
@@ -748,7 +748,7 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
     st = setup_cache(ctx, ctx->cache_b, ctx->pool_b, n_b, P.b_slot_bytes);
     if (st) return st;
   }
-  if (P.cz) {
+  if (P.embed) {
     st = reserve_oz_work(ctx, ns);
     if (st) return st;
   }
@@ -842,7 +842,7 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         if (!P.ozaki) {
           const int64_t lda_t = P.opa == tmm::OP_N ? mi : kk;
           const int64_t ldb_t = P.opb == tmm::OP_N ? kk : nj;
-          st = P.cz ? complex_ozaki(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s,
+          st = P.embed ? embedded_ozaki(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s,
                                     sidx)
                     : launch_tile_gemm(ctx, P.opa, P.opb, mi, nj, kk, alpha, SA.ptr, lda_t, SB.ptr, ldb_t, bk, ct, ldct, s);
           if (st) return st;
@@ -920,7 +920,7 @@ static int gemm_resident(tmm_context* ctx, char trans_a, char trans_b, int64_t m
   ctx->stats.n_streams = 1;
   ctx->stats.path = (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE) ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
   ctx->stats.ozaki_slices = ctx->stats.path == TMM_PATH_OZAKI
-                                ? (ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES) : 0;
+                                ? (ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::oz_default_slices(ctx->dtype)) : 0;
   ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return st;
 }
@@ -966,8 +966,8 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
     if (cudaMemGetInfo(&freeb, &total) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "cudaMemGetInfo");
     size_t budget = freeb + ctx->pool_a.capacity + ctx->pool_b.capacity + ctx->pool_c.capacity + ctx->staging.capacity;
     if (ctx->memory_limit) budget = std::min(budget, ctx->memory_limit);
-    const tmm::TileChoice tc = tmm::autotune_tiles(ctx->dtype, ozaki, ctx->ozaki_slices > 0 ? ctx->ozaki_slices
-                                                   : tmm::OZ_DEFAULT_SLICES, m, n, std::max<int64_t>(k, 1), budget,
+    const tmm::TileChoice tc = tmm::autotune_tiles(ctx->dtype, ctx->path == TMM_PATH_OZAKI, ctx->ozaki_slices > 0
+                                                   ? ctx->ozaki_slices : tmm::oz_default_slices(ctx->dtype), m, n, std::max<int64_t>(k, 1), budget,
                                                    ctx->max_tile_m, ctx->max_tile_n, ctx->max_tile_k);
     tm = tc.tm;
     tn = tc.tn;
@@ -988,8 +988,8 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   P.ntm = ntiles(m, tm); P.ntn = ntiles(n, tn); P.ntk = ntiles(k, tk);
   P.es = elem_size(ctx->dtype);
   P.ozaki = ozaki;
-  P.cz = ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_COMPLEX_DOUBLE;
-  P.slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+  P.embed = ctx->path == TMM_PATH_OZAKI && tmm::ozaki_embedded_dtype(ctx->dtype);
+  P.slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::oz_default_slices(ctx->dtype);
   P.engine = ctx->oz_engine;
   if (ozaki) {
     P.a_slot_bytes = tmm::ozaki_split_bytes(tm, tk, P.slices);
@@ -1017,12 +1017,12 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   ctx->stats.tile_n = tn;
   ctx->stats.tile_k = tk;
   ctx->stats.n_streams = (int)std::min<int64_t>(ctx->n_streams, P.ntm * P.ntn);
-  ctx->stats.path = (ozaki || P.cz) ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
-  ctx->stats.ozaki_slices = ozaki ? P.slices : 0;
+  ctx->stats.path = (ozaki || P.embed) ? TMM_PATH_OZAKI : TMM_PATH_NATIVE;
+  ctx->stats.ozaki_slices = (ozaki || P.embed) ? P.slices : 0;
   if (!st) st = run_gemm(ctx, P, alpha, a, ld_a, b, ld_b, beta, c, ld_c, copy_c_back != 0);
   int st2 = sync_all(ctx);  // returns with C final (the reference syncs the device: tiled_mm.cpp:602-604)
   if (!st) st = st2;
-  if (!st && (ozaki || P.cz)) st = check_oz_error(ctx);
+  if (!st && (ozaki || P.embed)) st = check_oz_error(ctx);
   unpin(pa);
   unpin(pb);
   unpin(pc);
@@ -1049,7 +1049,7 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream, as everywhere in CUDA
   if (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_DOUBLE && k > 0) {
     // split op(A) and op(B) in k-tiles of at most tile_k (per-k-tile scaling) into scratch, then multiply
-    const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::OZ_DEFAULT_SLICES;
+    const int slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::oz_default_slices(ctx->dtype);
     const int64_t tk = std::min<int64_t>(k, ctx->max_tile_k);
     const size_t sa = tmm::ozaki_split_bytes(m, tk, slices), sb = tmm::ozaki_split_bytes(n, tk, slices);
     const size_t sa_al = (sa + 255) / 256 * 256;
@@ -1075,10 +1075,10 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
     }
     return TMM_SUCCESS;
   }
-  if (ctx->path == TMM_PATH_OZAKI && ctx->dtype == TMM_COMPLEX_DOUBLE) {
+  if (ctx->path == TMM_PATH_OZAKI && tmm::ozaki_embedded_dtype(ctx->dtype)) {
     int st = reserve_oz_work(ctx, 1);
     if (st) return st;
-    return complex_ozaki(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s, 0);
+    return embedded_ozaki(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s, 0);
   }
   return launch_tile_gemm(ctx, opa, opb, m, n, k, alpha, a, ld_a, b, ld_b, beta, c, ld_c, s);
 }

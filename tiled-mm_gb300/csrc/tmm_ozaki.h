@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tmm_c_api.h"
 #include "tmm_kernels.h"
 
 namespace tmm {
@@ -19,6 +20,12 @@ constexpr int OZ_K_ALIGN = 128;    // k is padded to whole k-blocks (bytes)
 constexpr int OZ_DIGIT_BITS = 5;   // |d| <= 2^(w-1) = 16: exact in int8 and in e4m3
 constexpr int OZ_MAX_SLICES = 20;
 constexpr int OZ_DEFAULT_SLICES = 13;
+// float and complex float contexts: 6 slices (30 bits per line) leave the product within a
+// few units of FP32 rounding, below the error of an FP32-accumulating GEMM
+constexpr int OZ_DEFAULT_SLICES_FLOAT = 6;
+inline int oz_default_slices(int dtype) {
+  return dtype == TMM_FLOAT || dtype == TMM_COMPLEX_FLOAT ? OZ_DEFAULT_SLICES_FLOAT : OZ_DEFAULT_SLICES;
+}
 
 // digit byte encodings
 enum OzEnc : int { OZ_ENC_INT8 = 0, OZ_ENC_E4M3 = 1 };
@@ -77,14 +84,18 @@ size_t ozaki_workspace_bytes(int engine);
 int64_t ozaki_pass_blocks(int engine);
 int64_t ozaki_k_block(int engine);
 
-// Complex double on the engine (tmm_ozaki_complex.cu): Ahat (2m x 2k, ld 2m) and Bhat
-// (2k x n, ld 2k) are the real embedding of op(A) and op(B) (op C conjugates), whose real
-// product T (2m x n) holds Re C on top of Im C; combine applies the complex alpha and beta'
-// (beta' = beta on the first k-tile, C not read when it is zero; 1 after).
-cudaError_t ozaki_complex_embed(const void* A, int64_t lda, Op opa, const void* B, int64_t ldb, Op opb, int64_t m,
-                                int64_t n, int64_t k, double* Ahat, double* Bhat, cudaStream_t s);
-cudaError_t ozaki_complex_combine(int64_t m, int64_t n, const double* alpha, const double* beta, bool first,
-                                  const double* T, void* C, int64_t ldc, cudaStream_t s);
+// Float, complex float and complex double on the engine (tmm_ozaki_embed.cu).  embed writes
+// the real FP64 embedding of op(A) and op(B) (op C conjugates): for float Ahat = op(A)
+// (m x k, ld m) and Bhat = op(B) (k x n, ld k); for complex Ahat = [[Re, -Im], [Im, Re]]
+// of op(A) (2m x 2k, ld 2m) and Bhat = [Re; Im] of op(B) (2k x n, ld 2k), whose real
+// product T (2m x n) holds Re C on top of Im C.  combine writes C = alpha T + beta' C in
+// double, rounded once to the context's type (beta' = beta on the first k-tile, C not
+// read when it is zero; 1 after); alpha and beta point to scalars of the context's type.
+bool ozaki_embedded_dtype(int dtype);
+cudaError_t ozaki_embed(int dtype, const void* A, int64_t lda, Op opa, const void* B, int64_t ldb, Op opb, int64_t m,
+                        int64_t n, int64_t k, double* Ahat, double* Bhat, cudaStream_t s);
+cudaError_t ozaki_combine(int dtype, int64_t m, int64_t n, const void* alpha, const void* beta, bool first,
+                          const double* Tm, void* C, int64_t ldc, cudaStream_t s);
 
 // sets the message that tmm_last_error(NULL) returns on the calling thread (tmm_core.cpp)
 void set_last_error_message(const char* msg);

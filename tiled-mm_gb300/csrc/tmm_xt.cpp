@@ -42,10 +42,8 @@ int xt_gemm(tmm_xt* h, int dtype, int transa, int transb, int64_t m, int64_t n, 
     tmm_set_tile_policy(ctx, TMM_TILE_POLICY_FIXED);  // cublasXt tiles by the block dimension
   }
   h->last = ctx;
-  if (dtype == TMM_DOUBLE) {
-    const int st = tmm_set_path(ctx, h->path, h->slices);
-    if (st) return st;
-  }
+  const int st = tmm_set_path(ctx, h->path, h->slices);
+  if (st) return st;
   return tmm_gemm(ctx, op_char(transa), op_char(transb), m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, 1, 1);
 }
 
