@@ -83,6 +83,11 @@ WORKLOADS = {
                        path="batched", tiles=(4096, 4096, 4096), streams=2,
                        desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
                             "uniform[-1,1), pinned host buffers, one persistent launch in a captured CUDA graph"),
+    "batched512_ozaki": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
+                             path="batched", ozaki=True, tiles=(4096, 4096, 4096), streams=2,
+                             desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
+                                  "uniform[-1,1), pinned host buffers, captured CUDA graph; FP64 problems on the Ozaki "
+                                  "path at the slice count that meets the native batch's error metric"),
     "native4096": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=1.0, kind=0, param=0.0,
                        path="native", tiles=(2048, 2048, 2048), streams=2,
                        desc="FP64 GEMM m=n=k=4096 NN, uniform[-1,1), alpha=beta=1, tiles 2048, 2 streams"),
@@ -425,11 +430,13 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     return result
 
 
-def run_batched(args, rank, world, dist, log) -> dict:
+def run_batched(args, rank, world, dist, log, ozaki: bool = False) -> dict:
     """512 GEMMs, m, n, k log-uniform in [64, 4096], half FP64 / half FP32, random trans flags,
     uniform[-1,1) entries, page-locked host buffers: one persistent launch per call, captured
     (with its copies) into a CUDA graph on the first call and replayed; against a loop of the
-    plain per-problem path on the same problems."""
+    plain per-problem path on the same problems.  With ozaki, the FP64 problems run on the Ozaki
+    path at the smallest slice count whose error metric (max over the FP64 problems, sampled
+    entries) meets the native batch's, and the native batch is timed beside it."""
     import tiledmm as tmm
 
     rng = np.random.default_rng(1234 + rank)
@@ -453,18 +460,59 @@ def run_batched(args, rank, world, dist, log) -> dict:
         probs.append(dict(trans_a=ta, trans_b=tb, m=m, n=n, k=k, alpha=1.0, a=arrs[0], ld_a=ar, b=arrs[1], ld_b=br,
                           beta=0.0, c=arrs[2], ld_c=m))
         flops += 2.0 * m * n * k
+    f64 = [p for p in probs if p["a"].dtype == np.float64]
+    f64_flops = sum(2.0 * p["m"] * p["n"] * p["k"] for p in f64)
+    # error metric of the FP64 results: max over the 24 largest FP64 problems, 256 sampled entries each
+    err_probs = sorted(f64, key=lambda p: -p["m"] * p["n"] * p["k"])[:24]
+
+    def f64_error():
+        return max(tmm.error_metric(p["trans_a"], p["trans_b"], p["m"], p["n"], p["k"], 1.0, p["a"], p["ld_a"],
+                                    p["b"], p["ld_b"], 0.0, None, p["m"], p["c"], p["ld_c"], n_samples=256, seed=5)
+                   for p in err_probs)
+
+    def timed_batch(ctx):
+        times = []
+        for it in range(args.warmup + args.steps):
+            barrier(dist)
+            t0 = time.perf_counter()
+            tmm.gemm_batched(ctx, probs)
+            t1 = time.perf_counter()
+            if it >= args.warmup:
+                times.append(t1 - t0)
+        return max_over_ranks(dist, float(np.mean(times)))
+
     ctx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
-    times = []
-    for it in range(args.warmup + args.steps):
-        barrier(dist)
-        t0 = time.perf_counter()
-        tmm.gemm_batched(ctx, probs)
-        t1 = time.perf_counter()
-        if it >= args.warmup:
-            times.append(t1 - t0)
-    st = ctx.stats()
-    t_batch = max_over_ranks(dist, float(np.mean(times)))
-    log(f"batched: {t_batch * 1e3:.1f} ms per call, graph={st['batch_graph']}")
+    t_native = timed_batch(ctx)
+    st_native = ctx.stats()
+    e_native = f64_error()
+    log(f"batched native: {t_native * 1e3:.1f} ms per call, graph={st_native['batch_graph']}, error {e_native:.3g}")
+    out = {}
+    t_batch, st = t_native, st_native
+    if ozaki:
+        octx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+        octx.set_ozaki_engine(args.engine)
+        calib = {}
+        slices = args.slices
+        if not slices:
+            for s_try in range(7, 14):
+                octx.set_path(tmm.PATH_OZAKI, s_try)
+                tmm.gemm_batched(octx, probs)
+                calib[s_try] = f64_error()
+                if calib[s_try] <= e_native:
+                    slices = s_try
+                    break
+            slices = slices or 13
+        octx.set_path(tmm.PATH_OZAKI, slices)
+        t_batch = timed_batch(octx)
+        st = octx.stats()
+        e_oz = f64_error()
+        log(f"batched ozaki ({slices} slices): {t_batch * 1e3:.1f} ms per call, error {e_oz:.3g}")
+        out["ozaki"] = {"slices": slices, "calibration_error_metric": calib, "error_metric": e_oz,
+                        "seconds": t_batch, "engine": args.engine}
+        out["native_batch"] = {"tflops": world * flops / t_native / 1e12, "seconds": t_native, "error_metric": e_native,
+                               "graph": st_native["batch_graph"]}
+    else:
+        out["error_metric"] = e_native
     # the plain path, one call per problem (contexts per dtype, default tile policy)
     c64 = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
     c32 = tmm.make_context(np.float32, 2, 4096, 4096, 4096)
@@ -475,20 +523,31 @@ def run_batched(args, rank, world, dist, log) -> dict:
                  p["ld_b"], p["beta"], p["c"], p["ld_c"], pin_host_buffers=False, copy_c_back=True)
     t_loop = max_over_ranks(dist, time.perf_counter() - t0)
     log(f"loop of the plain path: {t_loop * 1e3:.1f} ms")
-    f64_flops = sum(2.0 * p["m"] * p["n"] * p["k"] for p in probs if p["a"].dtype == np.float64)
     for pa in keep:
         pa.free()
-    return {"value": world * flops / t_batch / 1e12, "ms_per_step": t_batch * 1e3, "gpu_launches": st["kernels"],
-            "e2e": {"value": world * flops / t_batch / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
-                    "d2h_bytes_per_step": st["d2h_bytes"], "note": "the batched call is host-to-host"},
-            "loop_of_plain_path": {"tflops": world * flops / t_loop / 1e12, "seconds": t_loop,
-                                   "speedup_of_batched": t_loop / t_batch},
-            "batch": {"problems": count, "flops": flops, "fp64_flops": f64_flops, "graph": st["batch_graph"]},
-            "roofline": {"bound": "tensor", "achieved": f64_flops / t_batch / 1e12,
-                         "peak": MEASURED_ENGINE_PEAKS["dmma_f64_tflops"], "unit": "TFLOP/s",
-                         "frac": f64_flops / t_batch / 1e12 / MEASURED_ENGINE_PEAKS["dmma_f64_tflops"],
-                         "traffic": None, "kernel": "grouped_kernel (FP64 DMMA items dominate)",
-                         "peak_source": "measured DMMA issue rate on this pool's GB300"}}
+    if ozaki:
+        pairs = out["ozaki"]["slices"] * (out["ozaki"]["slices"] + 1) // 2
+        lowp = pairs * f64_flops / t_batch / 1e12  # e4m3 slice-product rate, whole call (copies, FP32 half included)
+        roof = {"bound": "tensor", "achieved": lowp, "peak": MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"],
+                "unit": "TFLOP/s", "frac": lowp / MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"], "traffic": None,
+                "kernel": "oz_gemm_tc (FP64 problems, one launch per problem and k tile, 16 branch streams)",
+                "peak_source": "measured tcgen05 e4m3 issue rate on this pool's GB300",
+                "fp64_accurate_tflops_of_fp64_half": f64_flops / t_batch / 1e12}
+    else:
+        roof = {"bound": "tensor", "achieved": f64_flops / t_batch / 1e12,
+                "peak": MEASURED_ENGINE_PEAKS["dmma_f64_tflops"], "unit": "TFLOP/s",
+                "frac": f64_flops / t_batch / 1e12 / MEASURED_ENGINE_PEAKS["dmma_f64_tflops"],
+                "traffic": None, "kernel": "grouped_kernel (FP64 DMMA items dominate)",
+                "peak_source": "measured DMMA issue rate on this pool's GB300"}
+    res = {"value": world * flops / t_batch / 1e12, "ms_per_step": t_batch * 1e3, "gpu_launches": st["kernels"],
+           "e2e": {"value": world * flops / t_batch / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
+                   "d2h_bytes_per_step": st["d2h_bytes"], "note": "the batched call is host-to-host"},
+           "loop_of_plain_path": {"tflops": world * flops / t_loop / 1e12, "seconds": t_loop,
+                                  "speedup_of_batched": t_loop / t_batch},
+           "batch": {"problems": count, "flops": flops, "fp64_flops": f64_flops, "graph": st["batch_graph"]},
+           "roofline": roof}
+    res.update(out)
+    return res
 
 
 def _vendor_cublasxt():
@@ -735,10 +794,12 @@ def main() -> None:
             dist.destroy_process_group()
         return
     if w["path"] == "batched":
-        res = run_batched(args, rank, world, dist, log)
+        res = run_batched(args, rank, world, dist, log, ozaki=w.get("ozaki", False))
         if rank == 0:
             line = dict(base)
-            line["metric"] = "TFLOP/s of 512 uneven FP64/FP32 GEMMs (one persistent launch, graph replay)"
+            line["metric"] = ("FP64-accurate TFLOP/s of 512 uneven FP64/FP32 GEMMs (FP64 problems on the Ozaki path, "
+                              "graph replay)" if w.get("ozaki") else
+                              "TFLOP/s of 512 uneven FP64/FP32 GEMMs (one persistent launch, graph replay)")
             line["dtype"] = "f64+f32"
             line.update(res)
             print(json.dumps(line), flush=True)

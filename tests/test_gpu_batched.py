@@ -142,3 +142,85 @@ def test_batch_rejects_complex(tmm):
     with pytest.raises(RuntimeError, match="GPU ERROR"):
         tmm.gemm_batched(ctx, [dict(trans_a="N", trans_b="N", m=2, n=2, k=2, alpha=1.0, a=a, ld_a=2, b=a, ld_b=2,
                                     beta=0.0, c=a, ld_c=2)])
+
+
+# ---------------------------------------------------------------- FP64 problems on the Ozaki path
+def ozaki_expected(oracle, p, c0, slices, tk, eng):
+    """The oracle's Ozaki product with k tiles of tk (what tmm_gemm_device computes)."""
+    from oracle_lib import ozaki_oracle
+
+    want = c0.copy()
+    ta = "T" if p["trans_a"] == "C" else p["trans_a"]
+    tb = "T" if p["trans_b"] == "C" else p["trans_b"]
+    if p["k"] == 0:
+        return expected(oracle, p, c0)
+    return ozaki_oracle(oracle, ta, tb, p["m"], p["n"], p["k"], p["alpha"], p["a"], p["ld_a"], p["b"], p["ld_b"],
+                        p["beta"], want, p["ld_c"], slices, tk, eng["k_block"], eng["pass_blocks"])
+
+
+def check_ozaki(oracle, probs, c0s, slices, tk, eng):
+    """FP64 problems bit for bit the oracle's Ozaki product; FP32 problems as on the native path."""
+    for p, c0 in zip(probs, c0s):
+        if p["a"].dtype == np.float64:
+            np.testing.assert_array_equal(p["c"], ozaki_expected(oracle, p, c0, slices, tk, eng))
+        else:
+            check(oracle, [p], [c0])
+
+
+@pytest.mark.parametrize("engine", ["tcgen05", "imma"])
+def test_ozaki_batch_bit_exact(tmm, oracle, engine):
+    """On an Ozaki context the batch's FP64 problems (uneven shapes, N/T/C, k == 0, several k
+    tiles of max_tile_k) run on the engine and equal the oracle's Ozaki product bit for bit;
+    FP32 problems stay on the grouped kernel."""
+    rng = np.random.default_rng(11)
+    probs = make_batch(rng, 24, sizes=(1, 400), kmax=400)
+    c0s = [p["c"].copy() for p in probs]
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 160)
+    ctx.set_path(tmm.PATH_OZAKI, 7)
+    ctx.set_ozaki_engine(engine)
+    tmm.gemm_batched(ctx, probs)
+    st = ctx.stats()
+    assert st["path"] == tmm.PATH_OZAKI and st["ozaki_slices"] == 7
+    check_ozaki(oracle, probs, c0s, 7, 160, ctx.ozaki_engine())
+
+
+def test_ozaki_batch_graph_capture_replay_and_device_operands(tmm, oracle):
+    """Page-locked operands: the Ozaki launches are captured with the copies and replayed on new
+    data; the same batch from device operands gives the same bits."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(12)
+    keep = []
+
+    def pinned(x):
+        pa = tmm.PinnedArray(x.shape, x.dtype)
+        pa.array[:] = x
+        keep.append(pa)
+        return pa.array
+
+    probs = make_batch(rng, 20, pinned=pinned, sizes=(50, 500), kmax=600)
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 256)
+    ctx.set_path(tmm.PATH_OZAKI, 8)
+    eng = ctx.ozaki_engine()
+    c0s = [p["c"].copy() for p in probs]
+    tmm.gemm_batched(ctx, probs)
+    assert ctx.stats()["batch_graph"] == 1
+    check_ozaki(oracle, probs, c0s, 8, 256, eng)
+    for p in probs:
+        p["a"][:] = rng.uniform(-1, 1, p["a"].size)
+        p["c"][:] = rng.uniform(-1, 1, p["c"].size)
+    c0s = [p["c"].copy() for p in probs]
+    tmm.gemm_batched(ctx, probs)
+    assert ctx.stats()["batch_graph"] == 2
+    check_ozaki(oracle, probs, c0s, 8, 256, eng)
+    host_out = [p["c"].copy() for p in probs]
+    dev = []
+    for p, c0 in zip(probs, c0s):
+        d = dict(p)
+        d["a"], d["b"], d["c"] = (torch.from_numpy(x.copy()).cuda() for x in (p["a"], p["b"], c0))
+        d["dtype"] = p["a"].dtype
+        dev.append(d)
+    tmm.gemm_batched(ctx, dev, device_operands=True)
+    for d, h in zip(dev, host_out):
+        np.testing.assert_array_equal(d["c"].cpu().numpy(), h)
+    for pa in keep:
+        pa.free()

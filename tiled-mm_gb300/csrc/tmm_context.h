@@ -99,10 +99,18 @@ struct tmm_context {
 
   tmm::OzakiState* oz = nullptr;
 
+  // float and complex on the Ozaki engine: embedding, digit planes and real product, per stream slot
+  std::vector<tmm::GrowBuffer> cz_scratch;
+
+  // batched FP64 problems on the Ozaki path: digit planes per branch stream, the branch
+  // streams and their join events
+  tmm::GrowBuffer batch_oz_scratch;
+  std::vector<cudaStream_t> oz_branches;
+  std::vector<cudaEvent_t> oz_branch_done;
+  cudaEvent_t oz_fork = nullptr;
+
   // optional timing of the engine kernels (tmm_set_kernel_timing): event pairs recorded
   // on the launching stream around each launch, summed by tmm_get_kernel_time
-  // complex double on the Ozaki engine: embedding, digit planes and real product, per stream slot
-  std::vector<tmm::GrowBuffer> cz_scratch;
 
   bool ktime = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_pending, kt_free;

@@ -76,8 +76,8 @@ __device__ __forceinline__ uint32_t digit_byte(int d, int enc) {
 }
 
 constexpr int SP_LINES = 32, SP_L = 64, SP_THREADS = 256;
-constexpr int SP_KCHUNK = 512;        // k elements per digit block
-constexpr int MX_LINES = 256, MX_KCHUNK = 256;
+constexpr int SP_KCHUNK = 512;        // k elements per digit block (at most; a multiple of SP_L)
+constexpr int MX_LINES = 256, MX_KCHUNK = 256;  // k chunk of a block: at most MX_KCHUNK
 constexpr int EXP_NONE = (int)0x80808080;  // "no nonzero element yet" (byte pattern of the clearing memset)
 
 // frexp exponent of |x| from its IEEE bits (x != 0): 2^(e-1) <= |x| < 2^e
@@ -91,13 +91,15 @@ __device__ __forceinline__ int frexp_exponent_bits(uint64_t bits) {
 // line segment into exps[line] with one atomicMax (exps cleared to EXP_NONE).
 template <int TRANS>
 __global__ void __launch_bounds__(SP_THREADS)
-oz_linemax_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, int32_t* __restrict__ exps) {
-  const int64_t k0 = (int64_t)blockIdx.y * MX_KCHUNK;
-  const int64_t k1 = k0 + MX_KCHUNK < kk ? k0 + MX_KCHUNK : kk;
+oz_linemax_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, int32_t* __restrict__ exps,
+                  int kchunk) {
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = k0 + kchunk < kk ? k0 + kchunk : kk;
   if (TRANS == 0) {  // lines are contiguous across r: one line per thread, coalesced across the warp
     const int64_t r = (int64_t)blockIdx.x * MX_LINES + threadIdx.x;
     if (r >= rows) return;
     uint64_t mx = 0;
+#pragma unroll 8
     for (int64_t l = k0; l < k1; ++l) {
       const uint64_t b = (uint64_t)__double_as_longlong(X[r + l * ld]) & 0x7FFFFFFFFFFFFFFFull;
       mx = b > mx ? b : mx;
@@ -105,6 +107,7 @@ oz_linemax_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_
     if (mx) atomicMax(&exps[r], frexp_exponent_bits(mx));
   } else {  // line r is contiguous along l: a warp per line segment
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll 4
     for (int64_t r = (int64_t)blockIdx.x * MX_LINES + w; r < (int64_t)(blockIdx.x + 1) * MX_LINES && r < rows; r += 8) {
       uint64_t mx = 0;
       for (int64_t l = k0 + lane; l < k1; l += 32) {
@@ -155,12 +158,13 @@ struct DigitState {
   }
 };
 
-// Pass 2: digits of 32 lines x SP_KCHUNK k per block, staged through shared
+// Pass 2: digits of 32 lines x kchunk (<= SP_KCHUNK) k per block, staged through shared
 // memory so both the FP64 reads and the byte writes are coalesced.
 template <int TRANS>
 __global__ void __launch_bounds__(SP_THREADS)
 oz_digits_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t kk, uint8_t* __restrict__ digits,
-                 int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc, int blocked) {
+                 int32_t* __restrict__ exps, int64_t rows_pad, int64_t k_pad, int s, int enc, int blocked,
+                 int kchunk) {
   __shared__ double tile[SP_LINES][SP_L + 1];
   __shared__ int sexp[SP_LINES];
   const int tid = threadIdx.x;
@@ -173,8 +177,8 @@ oz_digits_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t
   __syncthreads();
   if (blockIdx.y == 0 && tid < SP_LINES) exps[r0 + tid] = sexp[tid];
   const size_t plane = (size_t)rows_pad * (size_t)k_pad;
-  const int64_t kbeg = (int64_t)blockIdx.y * SP_KCHUNK;
-  const int64_t kend = kbeg + SP_KCHUNK < k_pad ? kbeg + SP_KCHUNK : k_pad;
+  const int64_t kbeg = (int64_t)blockIdx.y * kchunk;
+  const int64_t kend = kbeg + kchunk < k_pad ? kbeg + kchunk : k_pad;
   for (int64_t l0 = kbeg; l0 < kend; l0 += SP_L) {
     if (TRANS == 0) {
       const int r = tid & 31, cg = tid >> 5;
@@ -376,24 +380,51 @@ oz_gemm_imma(const uint8_t* __restrict__ Ad, const int32_t* __restrict__ ea, int
 int64_t ozaki_pass_blocks(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_pass_blocks() : IM_PASS_BLOCKS; }
 int64_t ozaki_k_block(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_k_block() : IM_KB; }
 size_t ozaki_workspace_bytes(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_workspace_bytes() : 0; }
+size_t ozaki_workspace_bytes_for(int engine, int64_t m, int64_t n) {
+  return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_workspace_bytes_for(m, n) : 0;
+}
+cudaError_t ozaki_prepare(int engine) { return engine == OZ_ENGINE_TCGEN05 ? ozaki_tc_prepare() : cudaSuccess; }
+
+namespace {
+int split_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  });
+  return sms;
+}
+}  // namespace
 
 cudaError_t ozaki_split(const double* X, int64_t ld, Op trans, int64_t rows, int64_t kk, const OzakiSplit& out,
                         cudaStream_t s) {
   if (out.slices < 1 || out.slices > OZ_MAX_SLICES) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(out.exps, 0x80, (size_t)out.rows_pad * sizeof(int32_t), s);  // EXP_NONE
   if (e != cudaSuccess) return e;
+  // k chunks shrink (down to 32 / 64 elements) until the grid has about four blocks per SM:
+  // small operands are otherwise split by a few blocks that each walk a long k range
+  const int64_t want = 4 * (int64_t)split_sms();
   if (rows > 0 && kk > 0) {
-    dim3 gm((unsigned)((rows + MX_LINES - 1) / MX_LINES), (unsigned)((kk + MX_KCHUNK - 1) / MX_KCHUNK));
-    if (trans == OP_N) oz_linemax_kernel<0><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps);
-    else oz_linemax_kernel<1><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps);
+    const int64_t gx = (rows + MX_LINES - 1) / MX_LINES;
+    int kc = MX_KCHUNK;
+    while (kc > 32 && gx * ((kk + kc - 1) / kc) < want) kc /= 2;
+    dim3 gm((unsigned)gx, (unsigned)((kk + kc - 1) / kc));
+    if (trans == OP_N) oz_linemax_kernel<0><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps, kc);
+    else oz_linemax_kernel<1><<<gm, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.exps, kc);
   }
-  dim3 gd((unsigned)(out.rows_pad / SP_LINES), (unsigned)((out.k_pad + SP_KCHUNK - 1) / SP_KCHUNK));
+  const int64_t dx = out.rows_pad / SP_LINES;
+  int dc = SP_KCHUNK;
+  while (dc > SP_L && dx * ((out.k_pad + dc - 1) / dc) < want) dc /= 2;
+  dim3 gd((unsigned)dx, (unsigned)((out.k_pad + dc - 1) / dc));
   if (trans == OP_N)
     oz_digits_kernel<0><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                  out.slices, out.enc, out.blocked);
+                                                  out.slices, out.enc, out.blocked, dc);
   else
     oz_digits_kernel<1><<<gd, SP_THREADS, 0, s>>>(X, ld, rows, kk, out.digits, out.exps, out.rows_pad, out.k_pad,
-                                                  out.slices, out.enc, out.blocked);
+                                                  out.slices, out.enc, out.blocked, dc);
   return cudaGetLastError();
 }
 

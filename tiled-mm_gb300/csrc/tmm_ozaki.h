@@ -80,6 +80,11 @@ cudaError_t ozaki_gemm(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int6
                        cudaStream_t s);
 
 size_t ozaki_workspace_bytes(int engine);
+// workspace that one launch for an m x n product uses (at most ozaki_workspace_bytes)
+size_t ozaki_workspace_bytes_for(int engine, int64_t m, int64_t n);
+// one-time launch setup of the engine (attributes, occupancy, driver entry points), so
+// that later launches can be captured into a CUDA graph
+cudaError_t ozaki_prepare(int engine);
 // k-blocks (of the engine's k-block size) accumulated between two FP64 drains
 int64_t ozaki_pass_blocks(int engine);
 int64_t ozaki_k_block(int engine);
@@ -102,6 +107,8 @@ void set_last_error_message(const char* msg);
 
 // tcgen05 engine (tmm_tcgen05.cu)
 size_t ozaki_tc_workspace_bytes();
+size_t ozaki_tc_workspace_bytes_for(int64_t m, int64_t n);
+cudaError_t ozaki_tc_prepare();
 int64_t ozaki_tc_pass_blocks();
 int ozaki_tc_k_block();
 cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,

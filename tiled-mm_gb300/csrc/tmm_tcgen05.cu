@@ -279,6 +279,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// the same wait, with the loaded registers as operands so that no use of them is scheduled
+// before it
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.wait::ld.sync.aligned;"
+      : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]),
+        "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]),
+        "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]),
+        "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+      :
+      : "memory");
+}
 
 // ------------------------------------------------------------------ work sequence
 // Per tile: for g = s-1 .. 0, p = 0 .. g (q = g - p), kb = 0 .. nkb-1; a pass ends
@@ -299,6 +311,8 @@ struct Seq {
   __device__ bool pass_first() const { return used == 0; }
   // true when the current k-block closes a pass
   __device__ bool pass_last() const { return used + 1 == PASS_BLOCKS || (kb == nkb - 1 && p == g); }
+  // true on the tile's last k-block (diagonal 0 comes last)
+  __device__ bool tile_last() const { return g == 0 && kb == nkb - 1; }
   __device__ void next() {
     used = pass_last() ? 0 : used + 1;
     if (++kb == nkb) {
@@ -364,7 +378,95 @@ struct Params {
   int* err;
   int tiles_m, tiles_n;
   int pf;  // k-blocks the producer prefetches into L2 ahead of its loads (0: none)
+  uint32_t epi_hint;  // nanoseconds an epilogue warp may park per probe of a full accumulator
 };
+
+// FP64 arithmetic issues at about two operations per clock and SM on this GPU, so the
+// exact steps of the drain run on the integer pipes:
+// the pass sum S is an integer-valued FP32 (|S| < 2^24, exact by the pass limit), and
+// 2^-sh * S as a double is its sign and mantissa with the exponent rebased: no rounding.
+// (-0 becomes +0, which is what 0.0 + 2^-sh * S gives.)
+__device__ __forceinline__ double scaled_pass_sum(uint32_t fb, int sh) {
+  if ((fb & 0x7FFFFFFFu) == 0) return 0.0;
+  const uint32_t e = ((fb >> 23) & 0xFFu) + (1023 - 127) - (uint32_t)sh;  // >= 1023 - 50: normal
+  const uint32_t hi = (fb & 0x80000000u) | (e << 20) | ((fb & 0x7FFFFFu) >> 3);
+  return __hiloint2double((int)hi, (int)(fb << 29));
+}
+// scalbn(x, n), exactly: the exponent field is rebased when x and the result are normal;
+// zeros, subnormals, overflow and non-finite values take scalbn itself
+__device__ __forceinline__ double scalbn_fast(double x, int n) {
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) & 0x7FF;
+  if (e == 0 || e == 0x7FF || e + n < 1 || e + n > 0x7FE) return scalbn(x, n);
+  return __hiloint2double((int)((unsigned)hi + ((unsigned)n << 20)), __double2loint(x));
+}
+
+// Drain of one pass by one epilogue thread (tile row `row`, global row gi, first column
+// col0): acc = (first pass ? 0 : slot) + 2^(-5g) * S for the 256 columns, read from TMEM
+// in chunks of 32; release() hands the accumulator back once its last chunk is in
+// registers.  The slot values of a chunk are loaded while its TMEM load is in flight.  On
+// the tile's last pass the sums go straight into the fused epilogue
+// C = alpha * 2^(e_i + f_j - 8) * acc + beta' * C (beta' = beta on the first k tile, C not
+// read when it is zero) instead of back to the slot; the loads of a chunk's exponents and
+// C values are issued together.  One FP64 add per element and pass (none on the first).
+template <typename Release>
+__device__ __forceinline__ void drain_pass(uint32_t tbase, double* __restrict__ slot, int row, int g, bool first_pass,
+                                           bool last, const Params& P, int64_t gi, int64_t col0, Release release) {
+  const int sh = OZ_DIGIT_BITS * g;
+  const bool row_ok = gi < P.m;
+  const int ei = last && row_ok ? P.ea[gi] : 0;
+#pragma unroll 1
+  for (int c = 0; c < BN / 32; ++c) {
+    uint32_t r[32];
+    double acc[32];
+    tmem_ld32(tbase + (uint32_t)(c * 32), r);
+    if (!first_pass) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[j] = slot[(size_t)(c * 32 + j) * BM + row];
+    }
+    tmem_ld_wait(r);
+    if (c == BN / 32 - 1) release();
+    if (first_pass) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[j] = scaled_pass_sum(r[j], sh);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[j] += scaled_pass_sum(r[j], sh);
+    }
+    if (!last) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) slot[(size_t)(c * 32 + j) * BM + row] = acc[j];
+      continue;
+    }
+    const int64_t gj0 = col0 + c * 32;
+    if (!row_ok || gj0 >= P.n) continue;
+    const int nv = P.n - gj0 < 32 ? (int)(P.n - gj0) : 32;
+    const bool read_c = !P.first || P.beta != 0.0;
+    const bool plain = P.first && P.beta == 0.0 && P.alpha == 1.0;  // C = 2^(e_i + f_j - 8) * acc
+    double* cp = P.C + gi + gj0 * P.ldc;
+#pragma unroll
+    for (int h = 0; h < 32; h += 16) {
+      int fj[16];
+      double cv[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        fj[j] = h + j < nv ? P.eb[gj0 + h + j] : 0;
+        cv[j] = read_c && h + j < nv ? cp[(int64_t)(h + j) * P.ldc] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (h + j >= nv) break;
+        const double t = scalbn_fast(acc[h + j], ei + fj[j] - 2 * (OZ_DIGIT_BITS - 1));
+        double out;
+        if (plain) out = t;
+        else if (!P.first) out = fma(P.alpha, t, cv[j]);
+        else if (P.beta != 0.0) out = fma(P.alpha, t, P.beta * cv[j]);
+        else out = P.alpha * t;
+        cp[(int64_t)(h + j) * P.ldc] = out;
+      }
+    }
+  }
+}
 
 // CM CTAs of a cluster compute the tiles (CM*g + r, n) for r = 0..CM-1: they need
 // the same B tile, of which each CTA loads 1/CM and multicasts it to all, so the
@@ -558,48 +660,22 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         if (!q.pass_last()) continue;
         // one lane waits, the warp follows: the TMEM loads below are warp-collective
         int okw = 1;
-        if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err, EPI_WAIT_HINT_NS) ? 1 : 0;
+        if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err, P.epi_hint) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
         __syncwarp();
         if (!ok) break;
         tc_fence_after();
-        const double wg = scalbn(1.0, -OZ_DIGIT_BITS * q.g);
         const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
-#pragma unroll 1
-        for (int c = 0; c < BN / 32; ++c) {
-          uint32_t r[32];
-          tmem_ld32(tbase + (uint32_t)(c * 32), r);
-          tmem_ld_wait();
-          if (c == BN / 32 - 1) {  // accumulator consumed: hand it back to the MMA warp
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
-          }
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            double* w = slot + (size_t)(c * 32 + j) * BM + row;
-            const double v = (double)__uint_as_float(r[j]);
-            *w = (first_pass ? 0.0 : *w) + wg * v;
-          }
-        }
+        const uint32_t tempty = tempty0 + 8 * buf;
+        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), P, (int64_t)tm * BM + row, (int64_t)tn * BN,
+                   [&] {  // accumulator consumed: hand it back to the MMA warp
+                     tc_fence_before();
+                     __syncwarp();
+                     if (lane == 0) mbar_arrive(tempty);
+                   });
         first_pass = false;
         tphase[buf] ^= 1;
         buf ^= 1;
-      }
-      if (!ok) break;
-      // fused epilogue: C = alpha * 2^(e_i + f_j - 8) * acc + beta' * C
-      const int64_t gi = (int64_t)tm * BM + row;
-      if (gi < P.m) {
-        const int ei = P.ea[gi];
-        for (int col = 0; col < BN; ++col) {
-          const int64_t gj = (int64_t)tn * BN + col;
-          if (gj >= P.n) break;
-          const double t = scalbn(slot[(size_t)col * BM + row], ei + P.eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
-          double* cp = P.C + gi + gj * P.ldc;
-          if (!P.first) *cp = fma(P.alpha, t, *cp);
-          else if (P.beta != 0.0) *cp = fma(P.alpha, t, P.beta * *cp);
-          else *cp = P.alpha * t;
-        }
       }
     }
   }
@@ -796,47 +872,22 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         int okw = 1;
         if (lane == 0)
           okw = mbar_wait_pair<false>(tfull0 + 8 * buf, tphase[buf], abort_flag, peer_abort, P.err, true,
-                                      EPI_WAIT_HINT_NS) ? 1 : 0;
+                                      P.epi_hint) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
         __syncwarp();
         if (!ok) break;
         tc_fence_after();
-        const double wg = scalbn(1.0, -OZ_DIGIT_BITS * q.g);
         const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
-#pragma unroll 1
-        for (int c = 0; c < BN / 32; ++c) {
-          uint32_t r[32];
-          tmem_ld32(tbase + (uint32_t)(c * 32), r);
-          tmem_ld_wait();
-          if (c == BN / 32 - 1) {
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive_cluster(lead_tempty0 + 8 * buf);
-          }
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            double* w = slot + (size_t)(c * 32 + j) * BM + row;
-            const double v = (double)__uint_as_float(r[j]);
-            *w = (first_pass ? 0.0 : *w) + wg * v;
-          }
-        }
+        const uint32_t tempty = lead_tempty0 + 8 * buf;
+        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), P, (int64_t)tm * PAIR_M + rank * 128 + row,
+                   (int64_t)tn * BN, [&] {
+                     tc_fence_before();
+                     __syncwarp();
+                     if (lane == 0) mbar_arrive_cluster(tempty);
+                   });
         first_pass = false;
         tphase[buf] ^= 1;
         buf ^= 1;
-      }
-      if (!ok) break;
-      const int64_t gi = (int64_t)tm * PAIR_M + rank * 128 + row;
-      if (gi < P.m) {
-        const int ei = P.ea[gi];
-        for (int col = 0; col < BN; ++col) {
-          const int64_t gj = (int64_t)tn * BN + col;
-          if (gj >= P.n) break;
-          const double t = scalbn(slot[(size_t)col * BM + row], ei + P.eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
-          double* cp = P.C + gi + gj * P.ldc;
-          if (!P.first) *cp = fma(P.alpha, t, *cp);
-          else if (P.beta != 0.0) *cp = fma(P.alpha, t, P.beta * *cp);
-          else *cp = P.alpha * t;
-        }
       }
     }
   }
@@ -892,12 +943,20 @@ int num_sms() {
 
 // Persistent launch: as many clusters as can be resident at once (a cluster's
 // CTAs must share a GPC), capped by the number of cluster tiles.
+struct LaunchSetup {
+  cudaError_t status = cudaSuccess;
+  int max_clusters = 0;
+};
+
+// one-time attribute and occupancy setup of a cluster form (kept out of stream capture by
+// ozaki_tc_prepare)
 template <int CM>
-cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
+const LaunchSetup& launch_setup() {
+  static LaunchSetup su;
   static std::once_flag once;
-  static cudaError_t setup = cudaSuccess;
-  static int max_clusters = 0;
   std::call_once(once, [] {
+    cudaError_t& setup = su.status;
+    int& max_clusters = su.max_clusters;
     setup = cudaFuncSetAttribute(oz_gemm_tc<CM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (setup != cudaSuccess) return;
     if (CM == 1) {
@@ -918,7 +977,14 @@ cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P
     setup = cudaOccupancyMaxActiveClusters(&max_clusters, oz_gemm_tc<CM>, &cfg);
     if (setup == cudaSuccess && max_clusters <= 0) setup = cudaErrorInvalidConfiguration;
   });
-  if (setup != cudaSuccess) return setup;
+  return su;
+}
+
+template <int CM>
+cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
+  const LaunchSetup& su = launch_setup<CM>();
+  if (su.status != cudaSuccess) return su.status;
+  const int max_clusters = su.max_clusters;
   const int tiles_mg = (P.tiles_m + CM - 1) / CM;
   const int ctiles = tiles_mg * P.tiles_n;
   const int clusters = ctiles < max_clusters ? ctiles : max_clusters;
@@ -975,7 +1041,21 @@ cudaError_t launch_pair(const CUtensorMap& ma, const CUtensorMap& mb, const Para
 
 }  // namespace tc
 
+cudaError_t ozaki_tc_prepare() {
+  if (!tc::encode_fn()) return cudaErrorNotSupported;
+  cudaError_t e = tc::launch_setup<1>().status;
+  if (e == cudaSuccess) e = tc::launch_setup<2>().status;
+  if (e == cudaSuccess) e = tc::launch_setup<4>().status;
+  return e;
+}
+
 size_t ozaki_tc_workspace_bytes() { return (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
+size_t ozaki_tc_workspace_bytes_for(int64_t m, int64_t n) {
+  // a launch's grid is at most its tiles, rounded up to whole clusters of up to 4 (and at most one CTA per SM)
+  const int64_t tiles_m = (m + tc::BM - 1) / tc::BM, tiles_n = (n + tc::BN - 1) / tc::BN;
+  const int64_t ctas = std::min<int64_t>((int64_t)tc::num_sms(), (tiles_m + 3) / 4 * 4 * tiles_n);
+  return (size_t)ctas * tc::BM * tc::BN * sizeof(double);
+}
 int64_t ozaki_tc_pass_blocks() { return tc::PASS_BLOCKS; }
 int ozaki_tc_k_block() { return tc::KB; }
 
@@ -1007,6 +1087,8 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.work = work;
   P.err = err;
   P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
+  P.epi_hint = tc::EPI_WAIT_HINT_NS;
+  if (const char* env = getenv("TMM_TC_EPI_HINT_NS")) P.epi_hint = (uint32_t)(atoi(env) < 0 ? 0 : atoi(env));
   P.pf = 0;  // measured: any distance (4..32) slows the 8192^3 and 8192^2 x 32768 runs by 30-120 %
   if (const char* env = getenv("TMM_TC_PREFETCH")) P.pf = atoi(env) < 0 ? 0 : (atoi(env) > 64 ? 64 : atoi(env));
   // Engine form (TMM_TC_CLUSTER overrides): 1, 2, 4 = one-SM MMA on 128 x 256 tiles in
