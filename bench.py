@@ -530,7 +530,7 @@ def run_batched(args, rank, world, dist, log, ozaki: bool = False) -> dict:
         lowp = pairs * f64_flops / t_batch / 1e12  # e4m3 slice-product rate, whole call (copies, FP32 half included)
         roof = {"bound": "tensor", "achieved": lowp, "peak": MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"],
                 "unit": "TFLOP/s", "frac": lowp / MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"], "traffic": None,
-                "kernel": "oz_gemm_tc (FP64 problems, one launch per problem and k tile, 16 branch streams)",
+                "kernel": "oz_gemm_tc (FP64 problems: one launch per problem and k tile, a branch stream per problem)",
                 "peak_source": "measured tcgen05 e4m3 issue rate on this pool's GB300",
                 "fp64_accurate_tflops_of_fp64_half": f64_flops / t_batch / 1e12}
     else:
