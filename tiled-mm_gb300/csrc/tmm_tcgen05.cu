@@ -379,6 +379,7 @@ struct Params {
   int tiles_m, tiles_n;
   int pf;  // k-blocks the producer prefetches into L2 ahead of its loads (0: none)
   uint32_t epi_hint;  // nanoseconds an epilogue warp may park per probe of a full accumulator
+  int group_m;        // tile rows (of 128) per band of the tile order
 };
 
 // FP64 arithmetic issues at about two operations per clock and SM on this GPU, so the
@@ -489,7 +490,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   const int cluster_id = blockIdx.x / CM, num_clusters = gridDim.x / CM;
   const int tiles_mg = (P.tiles_m + CM - 1) / CM;  // cluster tile rows (a last partial group computes padding)
   const int total_ctiles = tiles_mg * P.tiles_n;
-  const int group = GROUP_M / CM > 0 ? GROUP_M / CM : 1;
+  const int group = P.group_m / CM > 0 ? P.group_m / CM : 1;
   constexpr uint16_t MASK = (uint16_t)((1u << CM) - 1);
   constexpr int B_SLICE = BN / CM;  // rows of B this CTA loads and multicasts
   constexpr int B_BOX = B_SLICE < OZ_BLOCK ? B_SLICE : OZ_BLOCK;  // a box stays inside one 128-line block
@@ -722,7 +723,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   const uint32_t peer_abort = mapa(smem_u32((const void*)abort_flag), rank ^ 1u);
   const int pair_id = blockIdx.x >> 1, num_pairs = gridDim.x >> 1;
   const int total_tiles = P.tiles_m * P.tiles_n;  // tiles_m counts 256-row tiles here
-  constexpr int group = GROUP_M / 2;
+  const int group = P.group_m / 2 > 0 ? P.group_m / 2 : 1;
   constexpr uint16_t BOTH = 3;
 
   if (threadIdx.x == 0) {
@@ -1087,6 +1088,8 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.work = work;
   P.err = err;
   P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
+  P.group_m = tc::GROUP_M;
+  if (const char* env = getenv("TMM_TC_GROUP_M")) P.group_m = atoi(env) < 1 ? 1 : (atoi(env) > 256 ? 256 : atoi(env));
   P.epi_hint = tc::EPI_WAIT_HINT_NS;
   if (const char* env = getenv("TMM_TC_EPI_HINT_NS")) P.epi_hint = (uint32_t)(atoi(env) < 0 ? 0 : atoi(env));
   P.pf = 0;  // measured: any distance (4..32) slows the 8192^3 and 8192^2 x 32768 runs by 30-120 %
