@@ -374,12 +374,15 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
     result["e2e"] = {"value": world * flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": st["h2d_bytes"],
                      "d2h_bytes_per_step": st["d2h_bytes"], "seconds_per_step": t_e2e,
-                     "host_buffers": ("pageable, registered inside each call" if w.get("pin") else "pageable")
+                     "host_buffers": ("pageable, registered inside each call" if w.get("pin") else
+                                      "pageable, not registered (copy kernels when the GPU reads host memory "
+                                      "through the host page tables)")
                      if pageable else "pinned (cudaHostAlloc)",
                      "copy_c_back": copy_back, "steps": args.e2e_steps,
                      "step_seconds": [round(x, 4) for x in e2e_times],
                      "engine_kernel_seconds_per_step": e2e_kernel_s / max(1, args.e2e_steps),
                      "clocks": e2e_clk.summary()}
+    result["e2e"]["direct_bytes_per_step"] = st["direct_bytes"]
     result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"], st["n_streams"]]
     result["e2e_tiles_loaded"] = st["tiles_loaded"]
     hctx.close()
@@ -743,11 +746,15 @@ def main() -> None:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--tiles", default="", help="tile_m,tile_n,tile_k of the context (overrides the workload's)")
+    ap.add_argument("--pin", default="workload", choices=["workload", "on", "off"],
+                    help="pin_host_buffers of the end-to-end call (default: the workload's)")
     ap.add_argument("--sweep-sizes", default="4000,6000,8000,10000,12000,14000,16000,18000,20000")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload], engine=args.engine)
     if args.tiles:
         w["tiles"] = tuple(int(x) for x in args.tiles.split(","))
+    if args.pin != "workload":
+        w["pin"] = args.pin == "on"
     rank, world, local, dist = dist_setup(args.gpus)
     log = (lambda s: print(s, file=sys.stderr, flush=True)) if rank == 0 else (lambda s: None)
     config = {"workload": w["desc"], "m": w["m"], "n": w["n"], "k": w["k"], "trans": w["ta"] + w["tb"],

@@ -221,6 +221,10 @@ typedef struct tmm_stats {
   int path, ozaki_slices;
   double seconds;         /* host wall time of the last call */
   int batch_graph;        /* last tmm_gemm_batched: 0 no graph, 1 captured, 2 replayed */
+  int direct_host;        /* TMM_DIRECT_HOST=1 and the GPU reads and writes pageable host memory through
+                             the host page tables: unregistered host tiles are copied by kernel */
+  uint64_t direct_bytes;  /* bytes of the last call copied by kernel between unregistered host memory and
+                             the device (the rest of h2d_bytes / d2h_bytes went through the copy engines) */
 } tmm_stats;
 
 int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);

@@ -163,6 +163,36 @@ def test_pinned_and_pageable_host_buffers(tmm):
     pa.free()
 
 
+@pytest.mark.parametrize("ozaki", [False, True])
+@pytest.mark.parametrize("copy_c_back", [True, False])
+def test_pageable_buffers_copied_by_kernel(tmm, monkeypatch, ozaki, copy_c_back):
+    """Unregistered (pageable) host buffers with pin_host_buffers == false and TMM_DIRECT_HOST=1:
+    on a GPU that reads host memory through the host page tables, A, B and C tiles move by copy
+    kernels (uneven tiles, padded leading dimensions, beta != 0); the result equals the
+    copy-engine path's (the default) bit for bit."""
+    rng = np.random.default_rng(61)
+    m, n, k = 333, 210, 275
+    a, lda, b, ldb, c, ldc = make_problem(rng, "T", "N", m, n, k, pad=3)
+
+    def call():
+        ctx = tmm.make_context(np.float64, 2, 128, 96, 100)
+        if ozaki:
+            ctx.set_path(tmm.PATH_OZAKI, 7)
+        out = run(tmm, ctx, "T", "N", m, n, k, 0.5, a, lda, b, ldb, -1.5, c.copy(), ldc, pin=False,
+                  copy_c_back=copy_c_back)
+        return out, ctx.stats()
+
+    monkeypatch.setenv("TMM_DIRECT_HOST", "1")
+    got, st = call()
+    monkeypatch.delenv("TMM_DIRECT_HOST")
+    want, st0 = call()
+    np.testing.assert_array_equal(got, want)
+    assert st0["direct_bytes"] == 0 and st0["direct_host"] == 0
+    if st["direct_host"]:
+        moved = st["h2d_bytes"] + (st["d2h_bytes"] if copy_c_back else 0)
+        assert st["direct_bytes"] == moved > 0
+
+
 def test_repeated_calls_are_deterministic_and_buffers_grow_only(tmm):
     rng = np.random.default_rng(7)
     ctx = tmm.make_context(np.float64, 2, 256, 256, 256)

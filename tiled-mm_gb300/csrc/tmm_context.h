@@ -75,6 +75,9 @@ struct tmm_context {
   int ozaki_slices = 0;
   int tile_policy = TMM_TILE_POLICY_REFERENCE;
   size_t memory_limit = 0;
+  // TMM_DIRECT_HOST=1 and the GPU reads and writes ordinary (pageable) host memory through the
+  // host page tables: tiles of unregistered host buffers are copied by kernel
+  bool direct_host = false;
 
   std::vector<cudaStream_t> streams;  // compute streams
   cudaStream_t h2d = nullptr;         // host -> device copies

@@ -284,6 +284,18 @@ extern "C" int tmm_create(int dtype, int n_streams, int max_tile_m, int max_tile
   ctx->max_tile_k = max_tile_k;
   ctx->oz_engine = tmm::ozaki_default_engine();
   cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e == cudaSuccess) {
+    int pageable = 0, host_tables = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, ctx->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) !=
+            cudaSuccess)
+      pageable = host_tables = 0;
+    // opt-in: the copy engines already read pageable memory near the link rate here (190-202 GB/s),
+    // and copy kernels beside the slice-product engine slowed the out-of-core update by 9 %
+    const char* env = getenv("TMM_DIRECT_HOST");
+    ctx->direct_host = pageable && host_tables && env && env[0] == '1';
+    cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->prep, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking);
@@ -681,8 +693,36 @@ int setup_cache(tmm_context* ctx, tmm::TileCache& c, tmm::GrowBuffer& pool, size
 
 struct HostMat {
   const char* ptr;
-  int64_t ld;  // elements
+  int64_t ld;   // elements
+  bool direct;  // unregistered host memory that the GPU accesses directly: copied by kernel
 };
+
+// true for ordinary (unregistered) host memory on a GPU that reads it through the host page
+// tables (the NVLink-C2C systems): a copy-engine copy of it is staged through page-locked
+// buffers and returns only when the source is consumed, a copy kernel stays asynchronous
+bool host_direct(const tmm_context* ctx, const void* p) {
+  if (!ctx->direct_host || !p) return false;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeUnregistered;
+}
+
+// 2D copy (height rows of width bytes) on stream s: by kernel when `direct`, else by the
+// copy engines
+int copy2d(tmm_context* ctx, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t height,
+           cudaStream_t s, bool direct) {
+  if (direct) {
+    TMM_CUDA(ctx, tmm::copy2d_async(dst, dpitch, src, spitch, width, height, s));
+    ctx->stats.kernels++;
+    ctx->stats.direct_bytes += (uint64_t)width * (uint64_t)height;
+    return TMM_SUCCESS;
+  }
+  TMM_CUDA(ctx, cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDefault, s));
+  return TMM_SUCCESS;
+}
 
 // Brings tile `key` (stored sub-block rows r0.., cols c0.. of size rr x cc)
 // into the cache; returns the slot.  The copy waits for the evicted tile's
@@ -703,8 +743,9 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
   const char* src = h.ptr + ((size_t)r0 + (size_t)c0 * (size_t)h.ld) * P.es;
   if (!P.ozaki) {
     if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, s.last_use, 0));
-    TMM_CUDA(ctx, cudaMemcpy2DAsync(s.ptr, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
-                                    (size_t)cc, cudaMemcpyDefault, ctx->h2d));
+    int st = copy2d(ctx, s.ptr, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es, (size_t)cc, ctx->h2d,
+                    h.direct);
+    if (st) return st;
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));
   } else {
     // raw tile -> staging buffer (ring of 3) on the copy stream; split -> slot on the stream of
@@ -714,8 +755,9 @@ int fetch_tile(tmm_context* ctx, const Plan& P, tmm::TileCache& cache, int64_t k
     int turn = (*staging_turn)++ % 3;
     char* stage = (char*)ctx->staging.ptr + (size_t)turn * ((P.staging_bytes + 255) / 256 * 256);
     TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->staging_free[turn], 0));
-    TMM_CUDA(ctx, cudaMemcpy2DAsync(stage, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es,
-                                    (size_t)cc, cudaMemcpyDefault, ctx->h2d));
+    int st = copy2d(ctx, stage, (size_t)rr * P.es, src, (size_t)h.ld * P.es, (size_t)rr * P.es, (size_t)cc, ctx->h2d,
+                    h.direct);
+    if (st) return st;
     TMM_CUDA(ctx, cudaEventRecord(s.ready, ctx->h2d));  // reused below as "staged"
     TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.ready, 0));
     if (s.used) TMM_CUDA(ctx, cudaStreamWaitEvent(split_stream, s.last_use, 0));
@@ -786,7 +828,8 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
   }
 
   // everything queued on this context's streams starts after earlier work on them
-  HostMat A{(const char*)a, lda}, B{(const char*)b, ldb};
+  HostMat A{(const char*)a, lda, host_direct(ctx, a)}, B{(const char*)b, ldb, host_direct(ctx, b)};
+  const bool c_direct = host_direct(ctx, c);
   const char* Ch = (const char*)c;
   int staging_turn = 0;
   char one[16] = {0};  // the scalar 1 of the context's dtype (beta' of later k-tiles)
@@ -818,8 +861,9 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
         ldct = P.m;
       }
       if (beta_nz) {  // the C tile is read only when beta != 0 (tiled_mm.cpp:325-330, 425-431)
-        TMM_CUDA(ctx, cudaMemcpy2DAsync(ct, (size_t)ldct * P.es, Ch + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es,
-                                        (size_t)ldc * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDefault, s));
+        st = copy2d(ctx, ct, (size_t)ldct * P.es, Ch + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es,
+                    (size_t)ldc * P.es, (size_t)mi * P.es, (size_t)nj, s, c_direct);
+        if (st) return st;
         ctx->stats.h2d_bytes += (uint64_t)mi * (uint64_t)nj * P.es;
       }
       if (P.ntk == 0) {
@@ -869,9 +913,9 @@ int run_gemm(tmm_context* ctx, Plan& P, const void* alpha, const void* a, int64_
       if (copy_back) {  // result stream copies the finished tile back (tiled_mm.cpp:350-358)
         TMM_CUDA(ctx, cudaEventRecord(cs->done, s));
         TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h, cs->done, 0));
-        TMM_CUDA(ctx, cudaMemcpy2DAsync((char*)c + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es, (size_t)ldc * P.es,
-                                        ct, (size_t)ldct * P.es, (size_t)mi * P.es, (size_t)nj, cudaMemcpyDefault,
-                                        ctx->d2h));
+        st = copy2d(ctx, (char*)c + ((size_t)r0 + (size_t)c0 * (size_t)ldc) * P.es, (size_t)ldc * P.es, ct,
+                    (size_t)ldct * P.es, (size_t)mi * P.es, (size_t)nj, ctx->d2h, c_direct);
+        if (st) return st;
         TMM_CUDA(ctx, cudaEventRecord(cs->done, ctx->d2h));
         cs->used = true;
         ctx->stats.d2h_bytes += (uint64_t)mi * (uint64_t)nj * P.es;
@@ -937,6 +981,7 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: null context");
   auto t0 = std::chrono::steady_clock::now();
   ctx->stats = tmm_stats{};
+  ctx->stats.direct_host = ctx->direct_host ? 1 : 0;
   Plan P{};
   if (!parse_op(trans_a, ctx->dtype, &P.opa) || !parse_op(trans_b, ctx->dtype, &P.opb))
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm: trans must be one of N, T, C");
@@ -1041,6 +1086,7 @@ extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int
                                const void* beta, void* c, int64_t ld_c, void* stream) {
   if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: null context");
   ctx->stats = tmm_stats{};
+  ctx->stats.direct_host = ctx->direct_host ? 1 : 0;
   Op opa, opb;
   if (!parse_op(trans_a, ctx->dtype, &opa) || !parse_op(trans_b, ctx->dtype, &opb))
     return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_device: trans must be one of N, T, C");
@@ -1405,6 +1451,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
   if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: null context");
   auto t0 = std::chrono::steady_clock::now();
   ctx->stats = tmm_stats{};
+  ctx->stats.direct_host = ctx->direct_host ? 1 : 0;
   if (count < 0 || (count > 0 && !probs)) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_gemm_batched: bad count");
   if (count == 0) return TMM_SUCCESS;
   DeviceGuard dg(ctx->device);

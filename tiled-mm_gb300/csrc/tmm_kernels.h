@@ -38,4 +38,9 @@ cudaError_t launch_scale_c64(int64_t m, int64_t n, cplxd beta, cplxd* C, int64_t
 cudaError_t launch_fill_f64(double* X, int64_t rows, int64_t cols, int64_t ld, int kind, double param,
                             uint64_t seed, uint64_t id, cudaStream_t s);
 
+// 2D copy by kernel (height rows of width bytes, pitches in bytes) for host memory that the
+// GPU accesses through the host page tables (tmm_native.cu)
+cudaError_t copy2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t height,
+                         cudaStream_t s);
+
 }  // namespace tmm

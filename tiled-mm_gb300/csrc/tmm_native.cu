@@ -9,6 +9,8 @@
 //
 // FP32 and the two complex types use a register-blocked SIMT kernel (FFMA,
 // full FP32/FP64 accuracy, matching cuBLAS's default non-TF32 semantics).
+#include <algorithm>
+
 #include "tmm_datagen.h"
 #include "tmm_kernels.h"
 #include "tmm_sgemm_tile.cuh"
@@ -374,6 +376,45 @@ cudaError_t launch_fill_f64(double* X, int64_t rows, int64_t cols, int64_t ld, i
                             uint64_t seed, uint64_t id, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return cudaSuccess;
   fill_f64_kernel<<<152 * 8, 256, 0, s>>>(X, rows, cols, ld, kind, param, seed, id);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ host <-> device tile copies by kernel
+// A 2D copy (height rows of width bytes) done by loads and stores of the SMs, for host memory
+// that the GPU reads and writes through the host page tables: unlike a copy-engine copy from
+// pageable memory it needs no page-locked staging, and it stays asynchronous.  V is the
+// widest access that every address, pitch and width allows.
+template <typename V>
+__global__ void copy2d_kernel(char* __restrict__ dst, size_t dpitch, const char* __restrict__ src, size_t spitch,
+                              size_t nvec, size_t rows) {
+  const size_t total = nvec * rows;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i / nvec, v = i - r * nvec;
+    *reinterpret_cast<V*>(dst + r * dpitch + v * sizeof(V)) =
+        *reinterpret_cast<const V*>(src + r * spitch + v * sizeof(V));
+  }
+}
+
+cudaError_t copy2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t height,
+                         cudaStream_t s) {
+  if (width == 0 || height == 0) return cudaSuccess;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const uintptr_t bits = (uintptr_t)dst | (uintptr_t)src | dpitch | spitch | width;
+  const size_t vb = (bits & 15) == 0 ? 16 : (bits & 7) == 0 ? 8 : (bits & 3) == 0 ? 4 : 1;
+  const size_t nvec = width / vb, total = nvec * height;
+  const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)sms * 4);
+  switch (vb) {
+    case 16: copy2d_kernel<uint4><<<grid, 256, 0, s>>>((char*)dst, dpitch, (const char*)src, spitch, nvec, height); break;
+    case 8: copy2d_kernel<uint2><<<grid, 256, 0, s>>>((char*)dst, dpitch, (const char*)src, spitch, nvec, height); break;
+    case 4: copy2d_kernel<uint32_t><<<grid, 256, 0, s>>>((char*)dst, dpitch, (const char*)src, spitch, nvec, height); break;
+    default: copy2d_kernel<uint8_t><<<grid, 256, 0, s>>>((char*)dst, dpitch, (const char*)src, spitch, nvec, height);
+  }
   return cudaGetLastError();
 }
 

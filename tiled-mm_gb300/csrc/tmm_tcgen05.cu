@@ -278,9 +278,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-// the same wait, with the loaded registers as operands so that no use of them is scheduled
-// before it
+// wait for this thread's tcgen05.ld; the loaded registers are operands so that no use of
+// them is scheduled before it
 __device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.wait::ld.sync.aligned;"

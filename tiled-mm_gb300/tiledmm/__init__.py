@@ -112,7 +112,7 @@ class Stats(C.Structure):
     _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernels", C.c_uint64),
                 ("tiles_loaded", C.c_uint64), ("tiles_reused", C.c_uint64), ("tile_m", _ci), ("tile_n", _ci),
                 ("tile_k", _ci), ("n_streams", _ci), ("path", _ci), ("ozaki_slices", _ci), ("seconds", C.c_double),
-                ("batch_graph", _ci)]
+                ("batch_graph", _ci), ("direct_host", _ci), ("direct_bytes", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
