@@ -4,7 +4,7 @@ for page-locked host operands, device operands, and both autotuned FP32 tile sha
 import numpy as np
 import pytest
 
-from gpu_helpers import dense, make_problem, tol_for
+from gpu_helpers import dense, make_problem, op, tol_for
 from oracle_lib import oracle_gemm
 
 pytestmark = pytest.mark.gpu
@@ -146,34 +146,74 @@ def test_batch_rejects_complex(tmm):
 
 # ---------------------------------------------------------------- FP64 problems on the Ozaki path
 def ozaki_expected(oracle, p, c0, slices, tk, eng):
-    """The oracle's Ozaki product with k tiles of tk (what tmm_gemm_device computes)."""
+    """The oracle's Ozaki product with k tiles of tk (what tmm_gemm_device computes).  FP32
+    problems (alpha = 1): per k tile the product of the FP64 embedding, then T + beta C
+    (first k tile) or T + C in double, rounded to float after every k tile."""
     from oracle_lib import ozaki_oracle
 
-    want = c0.copy()
     ta = "T" if p["trans_a"] == "C" else p["trans_a"]
     tb = "T" if p["trans_b"] == "C" else p["trans_b"]
     if p["k"] == 0:
         return expected(oracle, p, c0)
-    return ozaki_oracle(oracle, ta, tb, p["m"], p["n"], p["k"], p["alpha"], p["a"], p["ld_a"], p["b"], p["ld_b"],
-                        p["beta"], want, p["ld_c"], slices, tk, eng["k_block"], eng["pass_blocks"])
+    if p["a"].dtype == np.float64:
+        return ozaki_oracle(oracle, ta, tb, p["m"], p["n"], p["k"], p["alpha"], p["a"], p["ld_a"], p["b"], p["ld_b"],
+                            p["beta"], c0.copy(), p["ld_c"], slices, tk, eng["k_block"], eng["pass_blocks"])
+    assert p["alpha"] == 1.0
+    m, n, k = p["m"], p["n"], p["k"]
+    A = op(p["a"].astype(np.float64), p["ld_a"], ta, m, k)
+    B = op(p["b"].astype(np.float64), p["ld_b"], tb, k, n)
+    beta = float(np.float32(p["beta"]))
+    C = dense(c0, p["ld_c"], m, n).copy()
+    for kt, k0 in enumerate(range(0, k, tk)):
+        kk = min(tk, k - k0)
+        t = np.zeros(m * n)
+        ozaki_oracle(oracle, "N", "N", m, n, kk, 1.0, np.asfortranarray(A[:, k0:k0 + kk]).flatten(order="F"), m,
+                     np.asfortranarray(B[k0:k0 + kk, :]).flatten(order="F"), kk, 0.0, t, m, slices, kk,
+                     eng["k_block"], eng["pass_blocks"])
+        T = t.reshape(n, m).T
+        Cw = C.astype(np.float64)
+        if kt == 0:
+            Cw = T + beta * Cw if beta != 0.0 else T
+        else:
+            Cw = T + Cw
+        C = Cw.astype(np.float32)
+    out = c0.copy()
+    dense(out, p["ld_c"], m, n)[:] = C
+    return out
 
 
-def check_ozaki(oracle, probs, c0s, slices, tk, eng):
-    """FP64 problems bit for bit the oracle's Ozaki product; FP32 problems as on the native path."""
+def ozaki_batch(rng, count, **kw):
+    """make_batch with alpha = 1 on the FP32 problems (their expected values are emulated exactly)."""
+    probs = make_batch(rng, count, **kw)
+    for p in probs:
+        if p["a"].dtype == np.float32:
+            p["alpha"] = 1.0
+    return probs
+
+
+def check_ozaki(oracle, probs, c0s, slices, tk, eng, f32_on_engine=False, slices_f32=6):
+    """FP64 problems bit for bit the oracle's Ozaki product with `slices`; FP32 problems the
+    same for their FP64 embedding with `slices_f32` when they run on the engine, else as on
+    the native path."""
     for p, c0 in zip(probs, c0s):
-        if p["a"].dtype == np.float64:
-            np.testing.assert_array_equal(p["c"], ozaki_expected(oracle, p, c0, slices, tk, eng))
+        if p["a"].dtype == np.float64 or f32_on_engine:
+            s = slices if p["a"].dtype == np.float64 else slices_f32
+            np.testing.assert_array_equal(p["c"], ozaki_expected(oracle, p, c0, s, tk, eng))
         else:
             check(oracle, [p], [c0])
 
 
 @pytest.mark.parametrize("engine", ["tcgen05", "imma"])
-def test_ozaki_batch_bit_exact(tmm, oracle, engine):
+@pytest.mark.parametrize("f32_on_engine", [False, True])
+def test_ozaki_batch_bit_exact(tmm, oracle, monkeypatch, engine, f32_on_engine):
     """On an Ozaki context the batch's FP64 problems (uneven shapes, N/T/C, k == 0, several k
     tiles of max_tile_k) run on the engine and equal the oracle's Ozaki product bit for bit;
-    FP32 problems stay on the grouped kernel."""
+    FP32 problems stay on the grouped kernel, or with TMM_BATCH_OZ_F32=1 run on the engine
+    through their FP64 embedding at the float default of 6 slices, also bit for bit."""
+    if f32_on_engine:
+        monkeypatch.setenv("TMM_BATCH_OZ_F32", "1")
     rng = np.random.default_rng(11)
-    probs = make_batch(rng, 24, sizes=(1, 400), kmax=400)
+    probs = ozaki_batch(rng, 24, sizes=(1, 400), kmax=400)
     c0s = [p["c"].copy() for p in probs]
     ctx = tmm.make_context(np.float64, 2, 4096, 4096, 160)
     ctx.set_path(tmm.PATH_OZAKI, 7)
@@ -181,7 +221,7 @@ def test_ozaki_batch_bit_exact(tmm, oracle, engine):
     tmm.gemm_batched(ctx, probs)
     st = ctx.stats()
     assert st["path"] == tmm.PATH_OZAKI and st["ozaki_slices"] == 7
-    check_ozaki(oracle, probs, c0s, 7, 160, ctx.ozaki_engine())
+    check_ozaki(oracle, probs, c0s, 7, 160, ctx.ozaki_engine(), f32_on_engine)
 
 
 def test_ozaki_batch_graph_capture_replay_and_device_operands(tmm, oracle):
@@ -197,7 +237,7 @@ def test_ozaki_batch_graph_capture_replay_and_device_operands(tmm, oracle):
         keep.append(pa)
         return pa.array
 
-    probs = make_batch(rng, 20, pinned=pinned, sizes=(50, 500), kmax=600)
+    probs = ozaki_batch(rng, 20, pinned=pinned, sizes=(50, 500), kmax=600)
     ctx = tmm.make_context(np.float64, 2, 4096, 4096, 256)
     ctx.set_path(tmm.PATH_OZAKI, 8)
     eng = ctx.ozaki_engine()

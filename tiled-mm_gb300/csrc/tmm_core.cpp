@@ -1285,17 +1285,47 @@ constexpr int BATCH_OZ_BRANCHES = 256;  // measured on 256 FP64 problems: 64 -> 
 
 struct BatchOzPlan {
   std::vector<std::vector<int>> branch;  // problem indices per branch, in launch order
-  std::vector<size_t> offset;            // scratch offset of each branch: [engine workspace][digit planes]
+  std::vector<size_t> offset;            // scratch offset of each branch: [engine workspace][problem scratch]
   std::vector<size_t> work_bytes;        // engine workspace of each branch
-  int slices = 0;
+  int slices = 0;      // FP64 problems
+  int slices_f32 = 0;  // FP32 problems (the product of their FP64 embedding)
   int kernels = 0;
 };
+
+// slice count of a batch problem's precision: the context's own count for problems of its
+// precision, the precision's default for the others
+int batch_slices(const tmm_context* ctx, int dtype) {
+  const bool ctx_single = ctx->dtype == TMM_FLOAT || ctx->dtype == TMM_COMPLEX_FLOAT;
+  const bool single = dtype == TMM_FLOAT;
+  return ctx->ozaki_slices > 0 && ctx_single == single ? ctx->ozaki_slices : tmm::oz_default_slices(dtype);
+}
+
+// device scratch of one batch problem on the Ozaki path, per k tile of tk: the digit planes
+// (FP64), or the FP64 embedding Ahat (m x tk), Bhat (tk x n), its product T (m x n) and their
+// digit planes (FP32)
+struct BatchOzScratch {
+  size_t ahat = 0, bhat = 0, t = 0, sa = 0, sb = 0;
+  size_t total() const { return ahat + bhat + t + sa + sb; }
+};
+BatchOzScratch batch_oz_scratch(const tmm::BatchProblem& d, int64_t tk, int slices) {
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  BatchOzScratch r;
+  if (d.dtype == TMM_FLOAT) {
+    r.ahat = up((size_t)d.m * (size_t)tk * 8);
+    r.bhat = up((size_t)tk * (size_t)d.n * 8);
+    r.t = up((size_t)d.m * (size_t)d.n * 8);
+  }
+  r.sa = up(tmm::ozaki_split_bytes(d.m, tk, slices));
+  r.sb = up(tmm::ozaki_split_bytes(d.n, tk, slices));
+  return r;
+}
 
 int plan_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const std::vector<int>& ids,
                      BatchOzPlan* plan, bool* moved) {
   *plan = BatchOzPlan{};
   if (ids.empty()) return TMM_SUCCESS;
-  plan->slices = ctx->ozaki_slices > 0 ? ctx->ozaki_slices : tmm::oz_default_slices(TMM_DOUBLE);
+  plan->slices = batch_slices(ctx, TMM_DOUBLE);
+  plan->slices_f32 = batch_slices(ctx, TMM_FLOAT);
   int branches = BATCH_OZ_BRANCHES;
   if (const char* env = getenv("TMM_BATCH_OZ_BRANCHES")) branches = std::max(1, std::min(1024, atoi(env)));
   const int nb = std::min<int>((int)ids.size(), branches);
@@ -1312,10 +1342,11 @@ int plan_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev
     load[(size_t)b] += cost(id);
     const tmm::BatchProblem& d = dev[(size_t)id];
     const int64_t tk = std::min<int64_t>(d.k, ctx->max_tile_k);
-    const size_t bytes = up(tmm::ozaki_split_bytes(d.m, tk, plan->slices)) + up(tmm::ozaki_split_bytes(d.n, tk, plan->slices));
-    need[(size_t)b] = std::max(need[(size_t)b], bytes);
+    const bool f32 = d.dtype == TMM_FLOAT;
+    need[(size_t)b] = std::max(need[(size_t)b], batch_oz_scratch(d, tk, f32 ? plan->slices_f32 : plan->slices).total());
     work[(size_t)b] = std::max(work[(size_t)b], up(tmm::ozaki_workspace_bytes_for(ctx->oz_engine, d.m, d.n)));
-    plan->kernels += 5 * (int)((d.k + tk - 1) / tk);  // two two-kernel splits and the product per k tile
+    // per k tile: two two-kernel splits and the product (+ two embeddings and the combine for FP32)
+    plan->kernels += (f32 ? 8 : 5) * (int)((d.k + tk - 1) / tk);
   }
   size_t total = 0;
   for (int b = 0; b < nb; ++b) {
@@ -1372,6 +1403,37 @@ int copy_problem_out(tmm_context* ctx, const tmm_batch_problem& h, const tmm::Ba
   return TMM_SUCCESS;
 }
 
+// One FP32 problem of a batch on the Ozaki path, per k tile: the FP64 embedding of op(A) and
+// op(B), their digit planes, the engine's product T and C = alpha T + beta' C in double,
+// rounded once to float (beta' = beta on the first k tile, 1 after), as tmm_gemm does for a
+// float context on the Ozaki path.  alpha and beta are the problem's, rounded to float.
+int enqueue_batch_ozaki_f32(tmm_context* ctx, const tmm::BatchProblem& d, int64_t tk, int slices, char* base,
+                            double* work, cudaStream_t bs) {
+  const BatchOzScratch sc = batch_oz_scratch(d, tk, slices);
+  double* Ahat = (double*)base;
+  double* Bhat = (double*)(base + sc.ahat);
+  double* T = (double*)(base + sc.ahat + sc.bhat);
+  char* SA = base + sc.ahat + sc.bhat + sc.t;
+  char* SB = SA + sc.sa;
+  const float alpha = (float)d.alpha, beta = (float)d.beta, one = 1.f;
+  for (int64_t k0 = 0, kt = 0; k0 < d.k; k0 += tk, ++kt) {
+    const int64_t kk = std::min(tk, d.k - k0);
+    const float* ab = d.opa == tmm::OP_N ? (const float*)d.a + k0 * d.lda : (const float*)d.a + k0;
+    const float* bb = d.opb == tmm::OP_N ? (const float*)d.b + k0 : (const float*)d.b + k0 * d.ldb;
+    tmm::OzakiSplit va = tmm::ozaki_split_view(SA, d.m, kk, slices, ctx->oz_engine);
+    tmm::OzakiSplit vb = tmm::ozaki_split_view(SB, d.n, kk, slices, ctx->oz_engine);
+    cudaError_t e = tmm::ozaki_embed(TMM_FLOAT, ab, d.lda, d.opa, bb, d.ldb, d.opb, d.m, d.n, kk, Ahat, Bhat, bs);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Ahat, d.m, tmm::OP_N, d.m, kk, va, bs);
+    if (e == cudaSuccess) e = tmm::ozaki_split(Bhat, kk, tmm::OP_T, d.n, kk, vb, bs);
+    if (e == cudaSuccess)
+      e = tmm::ozaki_gemm(va, vb, d.m, d.n, 1.0, 0.0, true, T, d.m, ctx->oz_engine, work, oz_error_word(ctx), bs);
+    if (e == cudaSuccess)
+      e = tmm::ozaki_combine(TMM_FLOAT, d.m, d.n, &alpha, kt == 0 ? &beta : &one, true, T, d.c, d.ldc, bs);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki launch");
+  }
+  return TMM_SUCCESS;
+}
+
 // Forks the branches from s and queues each branch's problems: with host operands
 // (host != nullptr) every problem copies its operands in on its branch right before its
 // split and its C out right after its product, so the host link overlaps the products of
@@ -1392,6 +1454,12 @@ int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& 
         if (st) return st;
       }
       const int64_t tk = std::min<int64_t>(d.k, ctx->max_tile_k);
+      if (d.dtype == TMM_FLOAT) {
+        int st = enqueue_batch_ozaki_f32(ctx, d, tk, plan.slices_f32, base, plan.work_bytes[b] ? work : nullptr, bs);
+        if (st) return st;
+        if (host && (st = copy_problem_out(ctx, host[id], d, bs))) return st;
+        continue;
+      }
       const size_t sa_al = (tmm::ozaki_split_bytes(d.m, tk, plan.slices) + 255) / 256 * 256;
       for (int64_t k0 = 0, kt = 0; k0 < d.k; k0 += tk, ++kt) {
         const int64_t kk = std::min(tk, d.k - k0);
@@ -1513,13 +1581,17 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
       p += ((size_t)(d.m * d.n) * es + 255) / 256 * 256;
     }
   }
-  // FP64 problems on the Ozaki path leave the grouped kernels' list (their records stay,
-  // empty) for per-problem engine launches on branch streams
+  // on the Ozaki path FP64 problems with k > 0 leave the grouped kernels' list (their records
+  // stay, empty) for per-problem engine launches on branch streams
   std::vector<int> oz_ids;
   std::vector<tmm::BatchProblem> grouped = dev;
+  // FP32 problems join with TMM_BATCH_OZ_F32=1: beside the Ozaki branches the grouped FP32
+  // kernel was faster (512 problems: 76.9 ms per call against 84.2 ms with them on the engine)
+  const char* f32_env = getenv("TMM_BATCH_OZ_F32");
+  const bool f32_on_engine = f32_env && f32_env[0] == '1';
   if (ctx->path == TMM_PATH_OZAKI)
     for (int i = 0; i < count; ++i)
-      if (dev[i].dtype == TMM_DOUBLE && dev[i].m > 0 && dev[i].n > 0 && dev[i].k > 0) {
+      if (dev[i].m > 0 && dev[i].n > 0 && dev[i].k > 0 && (dev[i].dtype == TMM_DOUBLE || f32_on_engine)) {
         oz_ids.push_back(i);
         grouped[i].m = grouped[i].n = 0;
       }
@@ -1548,7 +1620,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
   // the layout key: every field of every problem, plus the chosen variants
   std::vector<unsigned char> key((const unsigned char*)probs, (const unsigned char*)probs + sizeof(tmm_batch_problem) * count);
   for (auto& d : dev) key.push_back((unsigned char)d.variant);
-  for (int v : {ctx->path, oz.slices, ctx->oz_engine, ctx->max_tile_k}) {
+  for (int v : {ctx->path, oz.slices, oz.slices_f32, ctx->oz_engine, ctx->max_tile_k, (int)f32_on_engine}) {
     const unsigned char* vb = (const unsigned char*)&v;
     key.insert(key.end(), vb, vb + sizeof(v));
   }
