@@ -45,7 +45,7 @@ MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 157.9, "dmma_f64_tflops": 1.099,
 # DRAM bytes (read + write) per launch of the slice-product kernel on the device-resident path,
 # from one ncu capture of the workload's own command (profiles/oz_gemm_tc_ozaki32768.md):
 # (workload, launch m, n, k tile, slices) -> bytes
-MEASURED_TRAFFIC = {("ozaki32768", (32768, 32768, 16384), 11): 2.871e12}
+MEASURED_TRAFFIC = {("ozaki32768", (32768, 32768, 16384), 11): 2.605e12}
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
