@@ -196,3 +196,51 @@ def test_ozaki_oracle_accuracy_with_enough_slices(oracle):
     vals = got.reshape(n, m).T[ii, jj].copy()
     metric = oracle.tmmo_error_metric(len(ii), vals.ctypes.data, ref.ctypes.data, mag.ctypes.data, k)
     assert metric < 0.05
+
+
+def test_ozaki_complex_embedding_on_the_oracle(oracle):
+    """The real embedding [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B] multiplied by the real
+    Ozaki restatement gives the complex product: exact on Gaussian integers of one digit."""
+    rng = np.random.default_rng(8)
+    m, n, k = 9, 7, 40
+    A = rng.integers(-9, 10, (m, k)) + 1j * rng.integers(-9, 10, (m, k))
+    B = rng.integers(-9, 10, (k, n)) + 1j * rng.integers(-9, 10, (k, n))
+    ahat = np.block([[A.real, -A.imag], [A.imag, A.real]])
+    bhat = np.vstack([B.real, B.imag])
+    t = np.zeros(2 * m * n)
+    ozaki_oracle(oracle, "N", "N", 2 * m, n, 2 * k, 1.0, ahat.flatten(order="F"), 2 * m, bhat.flatten(order="F"),
+                 2 * k, 0.0, t, 2 * m, slices=2, tk=2 * k, kb=128, pass_blocks=512)
+    T = t.reshape(n, 2 * m).T
+    np.testing.assert_array_equal(T[:m] + 1j * T[m:], A @ B)
+
+
+@pytest.mark.parametrize("dist", ["uniform", "row_exponents"])
+def test_float_default_slices_beat_fp32_accumulation(oracle, dist):
+    """The float contexts' default of 6 slices on the FP64 embedding of FP32 operands, rounded
+    once to float, has a smaller componentwise error than an FP32-accumulating product, within
+    about one FP32 rounding of the result."""
+    rng = np.random.default_rng(12)
+    m, n, k = 48, 40, 1024
+    if dist == "uniform":
+        A = rng.uniform(-1, 1, (m, k)).astype(np.float32)
+        B = rng.uniform(-1, 1, (k, n)).astype(np.float32)
+    else:
+        A = (rng.uniform(-1, 1, (m, k)) * 2.0 ** rng.integers(-8, 9, (m, 1))).astype(np.float32)
+        B = (rng.uniform(-1, 1, (k, n)) * 2.0 ** rng.integers(-8, 9, (1, n))).astype(np.float32)
+    A64, B64 = A.astype(np.float64), B.astype(np.float64)
+    exact = A64 @ B64
+    den = np.abs(A64) @ np.abs(B64)
+    acc = np.zeros((m, n), np.float32)  # FP32 accumulation in k order
+    for l in range(k):
+        acc += np.outer(A[:, l], B[l, :])
+
+    def oz(slices):
+        c = np.zeros(m * n)
+        ozaki_oracle(oracle, "N", "N", m, n, k, 1.0, A64.flatten(order="F"), m, B64.flatten(order="F"), k, 0.0, c, m,
+                     slices=slices, tk=k, kb=128, pass_blocks=512)
+        return c.reshape(n, m).T.astype(np.float32).astype(np.float64)
+
+    err = lambda X: float(np.max(np.abs(X - exact) / den))  # noqa: E731
+    e_fp32, e6 = err(acc.astype(np.float64)), err(oz(6))
+    assert e6 < e_fp32 / 4
+    assert e6 <= 2 * 2.0 ** -24  # within about one FP32 rounding of the result
