@@ -23,6 +23,8 @@
 //
 // A second form (oz_gemm_tc_pair, selected with TMM_TC_CLUSTER=pair) runs the
 // same sequence on CTA pairs with tcgen05.mma.cta_group::2 on 256 x 256 tiles.
+// Neither form multicasts a copy: each CTA's TMA loads land in its own shared
+// memory only.
 // Digit planes are read in the blocked layout (tmm_ozaki.h): every box a stage
 // loads is one contiguous 16 KB block.
 #include <cuda.h>
@@ -46,6 +48,7 @@ constexpr int TMEM_COLS = 512;
 constexpr int64_t PASS_BLOCKS = 512;  // 512 * 128 = 65536 k terms per exact FP32 pass
 constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 constexpr unsigned long long WAIT_NS = 1000000000ull;  // one second per wait
+constexpr size_t WORK_HEADER = 256;  // bytes before the accumulator slots: the pacing counter
 // the epilogue waits a whole pass (tens of microseconds) for an accumulator: park, don't spin
 constexpr uint32_t EPI_WAIT_HINT_NS = 20000;
 
@@ -117,15 +120,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
-      : "memory");
-}
-
 // L2 prefetch of the box at (x, y): a hint, nothing waits for it
 __device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
   asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)map), "r"(x), "r"(y)
@@ -176,13 +170,6 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-// arrive on the same-offset mbarrier of every CTA in `mask` when this thread's MMAs complete
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
-               "h"(mask)
-               : "memory");
 }
 
 // ---- CTA-pair (cta_group::2) forms
@@ -379,7 +366,47 @@ struct Params {
   int pf;  // k-blocks the producer prefetches into L2 ahead of its loads (0: none)
   uint32_t epi_hint;  // nanoseconds an epilogue warp may park per probe of a full accumulator
   int group_m;        // tile rows (of 128) per band of the tile order
+  // Wave pacing: the producers publish their progress (one count per chunk of pace_chunk
+  // k-blocks) to *pace, and one that is more than pace_lag chunks ahead of the average CTA
+  // waits (at most pace_ns per chunk, then goes on: a hint, never an error), so that the
+  // co-resident CTAs stay at about the same (diagonal, pair, k-block) position of their
+  // tiles and the A and B blocks that a step shares are read from DRAM once.
+  unsigned long long* pace;
+  int pace_lag;  // 0: off
+  int pace_chunk;  // a power of two
+  uint32_t pace_ns;
 };
+
+__device__ __forceinline__ void red_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Called by a producer at the start of its chunk c (k-blocks counted over all its tiles; every
+// tile has the same sequence, so equal counts are equal positions).  seen caches the last value
+// read: when it already allows chunk c, a fresh read is issued for the next call and not waited on.
+__device__ __forceinline__ void pace_gate(const Params& P, unsigned long long c, unsigned long long ctas,
+                                          unsigned long long& seen) {
+  if (c > 0) red_add_u64(P.pace, 1ull);  // chunk c - 1 issued
+  if (c <= (unsigned long long)P.pace_lag) return;
+  const unsigned long long need = (c - (unsigned long long)P.pace_lag) * ctas;
+  if (seen >= need) {
+    seen = ld_relaxed_u64(P.pace);
+    return;
+  }
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    seen = ld_relaxed_u64(P.pace);
+    if (seen >= need || globaltimer() - t0 > P.pace_ns) return;
+    __nanosleep(256);
+  }
+}
+// a producer that has issued all its work lifts its weight off the others' gates
+constexpr unsigned long long PACE_DONE = 1ull << 40;
 
 // FP64 arithmetic issues at about two operations per clock and SM on this GPU, so the
 // exact steps of the drain run on the integer pipes:
@@ -468,12 +495,9 @@ __device__ __forceinline__ void drain_pass(uint32_t tbase, double* __restrict__ 
   }
 }
 
-// CM CTAs of a cluster compute the tiles (CM*g + r, n) for r = 0..CM-1: they need
-// the same B tile, of which each CTA loads 1/CM and multicasts it to all, so the
-// L2->SM operand traffic per CTA drops from 48 KB to 16 + 32/CM KB per k-block.
-// A stage is refilled only after every CTA's MMAs have read it (the empty
-// barrier counts one commit per CTA, sent by multicast).
-template <int CM>
+// One CTA per SM computes its 128 x 256 tiles alone: every TMA copy lands in
+// this CTA's own shared memory (no cluster, no multicast), and a stage is
+// refilled once this CTA's MMAs have read it.
 __global__ void __launch_bounds__(THREADS, 1)
 oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -485,19 +509,14 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
-  const int rank = CM > 1 ? (int)cluster_ctarank() : 0;
-  const int cluster_id = blockIdx.x / CM, num_clusters = gridDim.x / CM;
-  const int tiles_mg = (P.tiles_m + CM - 1) / CM;  // cluster tile rows (a last partial group computes padding)
-  const int total_ctiles = tiles_mg * P.tiles_n;
-  const int group = P.group_m / CM > 0 ? P.group_m / CM : 1;
-  constexpr uint16_t MASK = (uint16_t)((1u << CM) - 1);
-  constexpr int B_SLICE = BN / CM;  // rows of B this CTA loads and multicasts
-  constexpr int B_BOX = B_SLICE < OZ_BLOCK ? B_SLICE : OZ_BLOCK;  // a box stays inside one 128-line block
+  const int total_tiles = P.tiles_m * P.tiles_n;
+  const int group = P.group_m > 0 ? P.group_m : 1;
+  constexpr int B_BOX = OZ_BLOCK;  // a box stays inside one 128-line block of the blocked layout
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
       mbar_init(full0 + 8 * i, 1);
-      mbar_init(empty0 + 8 * i, CM);
+      mbar_init(empty0 + 8 * i, 1);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(tfull0 + 8 * i, 1);
@@ -513,7 +532,6 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   if (warp == 1) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
   tc_fence_before();
   __syncthreads();
-  if (CM > 1) cluster_sync();  // peers' barriers are initialised before any multicast lands
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
@@ -523,16 +541,17 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
-        int tmg, tn;
-        tile_coords(ct, tiles_mg, P.tiles_n, group, &tmg, &tn);
-        const int tm = tmg * CM + rank;
+      unsigned long long issued = 0, seen = 0;  // k-blocks issued in this launch; last pace count read
+      const unsigned long long chunk_mask = (unsigned long long)P.pace_chunk - 1;
+      for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
+        int tm, tn;
+        tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
         // f runs P.pf k-blocks ahead of q: its boxes are prefetched into L2 so that the
         // loads, issued when a stage frees up, find them there instead of in DRAM
-        const int64_t b0 = (int64_t)tn * BN + rank * B_SLICE;
+        const int64_t b0 = (int64_t)tn * BN;
         auto prefetch = [&](const Seq& f) {
           tma_prefetch_2d(&tmA, 0, box_y(f.p, (int64_t)tm * BM, f.kb, P.a_rows_pad, P.nkb));
-          for (int j = 0; j < B_SLICE / B_BOX; ++j)
+          for (int j = 0; j < BN / B_BOX; ++j)
             tma_prefetch_2d(&tmB, 0, box_y(f.g - f.p, b0 + j * B_BOX, f.kb, P.b_rows_pad, P.nkb));
         };
         Seq q, f;
@@ -543,18 +562,18 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             prefetch(f);
             f.next();
           }
+          if (P.pace_lag && (issued & chunk_mask) == 0) pace_gate(P, issued / P.pace_chunk, gridDim.x, seen);
+          ++issued;
           ok = mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
           if (!ok) break;
           const uint32_t fb = full0 + 8 * stage;
-          mbar_expect_tx(fb, STAGE_BYTES);  // own A + every CTA's B slice
+          mbar_expect_tx(fb, STAGE_BYTES);  // A box + the B boxes
           uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
           tma_load_2d(smem_u32(sa), &tmA, 0, box_y(q.p, (int64_t)tm * BM, q.kb, P.a_rows_pad, P.nkb), fb);
 #pragma unroll
-          for (int j = 0; j < B_SLICE / B_BOX; ++j) {
+          for (int j = 0; j < BN / B_BOX; ++j) {
             const int by = box_y(q.g - q.p, b0 + j * B_BOX, q.kb, P.b_rows_pad, P.nkb);
-            const uint32_t bdst = smem_u32(sa + A_BYTES + (rank * B_SLICE + j * B_BOX) * KB);
-            if (CM > 1) tma_load_2d_mc(bdst, &tmB, 0, by, fb, MASK);
-            else tma_load_2d(bdst, &tmB, 0, by, fb);
+            tma_load_2d(smem_u32(sa + A_BYTES + j * B_BOX * KB), &tmB, 0, by, fb);
           }
           if (++stage == STAGES) {
             stage = 0;
@@ -562,6 +581,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
           }
         }
       }
+      if (P.pace_lag) red_add_u64(P.pace, PACE_DONE);
       // drain: every issued copy has landed before the CTA may exit (bounded)
       for (int i = 0; i < STAGES; ++i) {
         (void)mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
@@ -585,7 +605,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       const uint32_t sa0 = smem_u32(smem);
       const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + A_BYTES);
       MmaCursor cur;
-      cur.start(cluster_id, total_ctiles, P.s, P.nkb);
+      cur.start(blockIdx.x, total_tiles, P.s, P.nkb);
       int stage = 0, buf = 0;
       uint32_t phase = 0, tph = 0;  // tph bit b: phase of accumulator b's full barrier
       uint64_t ad = ad0, bd = bd0;
@@ -601,7 +621,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         mma_f8(d_tmem, ad + 2, bd + 2, 1u);
         mma_f8(d_tmem, ad + 4, bd + 4, 1u);
         // ---- next k-block, while two MMAs are still queued
-        cur.next(num_clusters, total_ctiles, P.s, P.nkb);
+        cur.next(gridDim.x, total_tiles, P.s, P.nkb);
         const bool nvalid = cur.valid;
         const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
         const int nstage = stage + 1 == STAGES ? 0 : stage + 1;
@@ -609,9 +629,8 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
         const bool ready = nvalid && !nfirst && mbar_try_wait(full0 + 8 * nstage, nphase);
         mma_f8(d_tmem, ad + 6, bd + 6, 1u);
-        // the stage is free (in every CTA of the cluster) when these MMAs have read it
-        if (CM > 1) mma_commit_mc(empty0 + 8 * stage, MASK);
-        else mma_commit(empty0 + 8 * stage);
+        // the stage is free when these MMAs have read it
+        mma_commit(empty0 + 8 * stage);
         if (last) {
           mma_commit(tfull0 + 8 * buf);
           tph ^= 1u << buf;
@@ -650,10 +669,9 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     uint32_t tphase[2] = {0, 0};
     int buf = 0;
     bool ok = true;
-    for (int ct = cluster_id; ct < total_ctiles && ok; ct += num_clusters) {
-      int tmg, tn;
-      tile_coords(ct, tiles_mg, P.tiles_n, group, &tmg, &tn);
-      const int tm = tmg * CM + rank;
+    for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
+      int tm, tn;
+      tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
       bool first_pass = true;
       Seq q;
       for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
@@ -680,9 +698,8 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     }
   }
   tc_fence_before();
-  __syncwarp();  // lane 0 of warps 0 and 1 ran alone: the cluster barrier below is warp-collective
+  __syncwarp();  // lane 0 of warps 0 and 1 ran alone
   __syncthreads();
-  if (CM > 1) cluster_sync();  // no peer multicasts into this CTA after it leaves
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
@@ -754,6 +771,8 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
+      unsigned long long issued = 0, seen = 0;  // as in oz_gemm_tc: both CTAs of a pair publish
+      const unsigned long long chunk_mask = (unsigned long long)P.pace_chunk - 1;
       for (int ct = pair_id; ct < total_tiles && ok; ct += num_pairs) {
         int tm, tn;
         tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
@@ -771,6 +790,8 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             prefetch(f);
             f.next();
           }
+          if (P.pace_lag && (issued & chunk_mask) == 0) pace_gate(P, issued / P.pace_chunk, gridDim.x, seen);
+          ++issued;
           ok = mbar_wait_pair<false>(empty0 + 8 * stage, phase ^ 1, abort_flag, peer_abort, P.err);
           if (!ok) break;
           if (rank == 0) mbar_expect_tx(full0 + 8 * stage, 2 * PAIR_STAGE_BYTES);
@@ -784,6 +805,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
           }
         }
       }
+      if (P.pace_lag) red_add_u64(P.pace, PACE_DONE);
       // drain: every copy issued has been consumed before the CTA may exit (bounded)
       for (int i = 0; i < PAIR_STAGES; ++i) {
         (void)mbar_wait_pair<false>(empty0 + 8 * stage, phase ^ 1, abort_flag, peer_abort, P.err, false);
@@ -929,113 +951,84 @@ cudaError_t make_map(CUtensorMap* map, const OzakiSplit& X, int box_rows) {
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-int num_sms() {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  });
-  return sms;
-}
-
-// Persistent launch: as many clusters as can be resident at once (a cluster's
-// CTAs must share a GPC), capped by the number of cluster tiles.
-struct LaunchSetup {
+// Per-device launch set-up of both engine forms: the SM count, the opt-in to the large
+// dynamic shared memory (a function attribute is per device) and the pair form's
+// resident-cluster count.  Done once per device, with that device current, outside
+// any stream capture (ozaki_tc_prepare).
+struct DeviceSetup {
+  std::once_flag once;
   cudaError_t status = cudaSuccess;
-  int max_clusters = 0;
+  int sms = 0;
+  int max_pairs = 0;
 };
+constexpr int MAX_DEVICES = 64;
+DeviceSetup g_setup[MAX_DEVICES];
 
-// one-time attribute and occupancy setup of a cluster form (kept out of stream capture by
-// ozaki_tc_prepare)
-template <int CM>
-const LaunchSetup& launch_setup() {
-  static LaunchSetup su;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaError_t& setup = su.status;
-    int& max_clusters = su.max_clusters;
-    setup = cudaFuncSetAttribute(oz_gemm_tc<CM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
-    if (setup != cudaSuccess) return;
-    if (CM == 1) {
-      max_clusters = num_sms();
-      return;
-    }
+const DeviceSetup* device_setup() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return nullptr;
+  DeviceSetup& d = g_setup[dev];
+  std::call_once(d.once, [&d, dev] {
+    d.status = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (d.status != cudaSuccess) return;
+    if (d.sms <= 0) d.sms = 1;
+    d.status = cudaFuncSetAttribute(oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (d.status != cudaSuccess) return;
+    d.status = cudaFuncSetAttribute(oz_gemm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAIR_SMEM_BYTES);
+    if (d.status != cudaSuccess) return;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = CM;
+    at[0].val.clusterDim.x = 2;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3((unsigned)((num_sms() / CM) * CM));
+    cfg.gridDim = dim3((unsigned)((d.sms / 2) * 2));
     cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.dynamicSmemBytes = PAIR_SMEM_BYTES;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    setup = cudaOccupancyMaxActiveClusters(&max_clusters, oz_gemm_tc<CM>, &cfg);
-    if (setup == cudaSuccess && max_clusters <= 0) setup = cudaErrorInvalidConfiguration;
+    d.status = cudaOccupancyMaxActiveClusters(&d.max_pairs, oz_gemm_tc_pair, &cfg);
+    if (d.status == cudaSuccess && d.max_pairs <= 0) d.status = cudaErrorInvalidConfiguration;
   });
-  return su;
+  return &d;
 }
 
-template <int CM>
+int num_sms() {
+  const DeviceSetup* d = device_setup();
+  return d && d->status == cudaSuccess ? d->sms : 1;
+}
+
+// Persistent launch: one CTA per SM, at most one per tile.
 cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
-  const LaunchSetup& su = launch_setup<CM>();
-  if (su.status != cudaSuccess) return su.status;
-  const int max_clusters = su.max_clusters;
-  const int tiles_mg = (P.tiles_m + CM - 1) / CM;
-  const int ctiles = tiles_mg * P.tiles_n;
-  const int clusters = ctiles < max_clusters ? ctiles : max_clusters;
-  if ((size_t)clusters * CM > (size_t)num_sms()) return cudaErrorInvalidConfiguration;  // workspace has one slot per SM
-  if (CM == 1) {
-    oz_gemm_tc<1><<<clusters, THREADS, SMEM_BYTES, s>>>(ma, mb, P);
-    return cudaGetLastError();
-  }
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CM;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3((unsigned)(clusters * CM));
-  cfg.blockDim = dim3(THREADS);
-  cfg.dynamicSmemBytes = SMEM_BYTES;
-  cfg.stream = s;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, oz_gemm_tc<CM>, ma, mb, P);
+  const DeviceSetup* d = device_setup();
+  if (!d) return cudaErrorInvalidDevice;
+  if (d->status != cudaSuccess) return d->status;
+  const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
+  const int ctas = tiles < d->sms ? (int)tiles : d->sms;  // the workspace has one slot per SM
+  oz_gemm_tc<<<ctas, THREADS, SMEM_BYTES, s>>>(ma, mb, P);
+  return cudaGetLastError();
 }
 
 // Persistent launch of the pair engine: clusters of 2 CTAs, as many as can be resident.
 cudaError_t launch_pair(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P, cudaStream_t s) {
-  static std::once_flag once;
-  static cudaError_t setup = cudaSuccess;
-  static int max_pairs = 0;
+  const DeviceSetup* d = device_setup();
+  if (!d) return cudaErrorInvalidDevice;
+  if (d->status != cudaSuccess) return d->status;
+  const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
+  const int pairs = tiles < d->max_pairs ? (int)tiles : d->max_pairs;
+  if ((size_t)pairs * 2 > (size_t)d->sms) return cudaErrorInvalidConfiguration;  // workspace has one slot per SM
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = 2;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(pairs * 2));
   cfg.blockDim = dim3(THREADS);
   cfg.dynamicSmemBytes = PAIR_SMEM_BYTES;
+  cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  std::call_once(once, [&cfg] {
-    setup = cudaFuncSetAttribute(oz_gemm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAIR_SMEM_BYTES);
-    if (setup != cudaSuccess) return;
-    cfg.gridDim = dim3((unsigned)((num_sms() / 2) * 2));
-    setup = cudaOccupancyMaxActiveClusters(&max_pairs, oz_gemm_tc_pair, &cfg);
-    if (setup == cudaSuccess && max_pairs <= 0) setup = cudaErrorInvalidConfiguration;
-  });
-  if (setup != cudaSuccess) return setup;
-  const int tiles = P.tiles_m * P.tiles_n;
-  const int pairs = tiles < max_pairs ? tiles : max_pairs;
-  if ((size_t)pairs * 2 > (size_t)num_sms()) return cudaErrorInvalidConfiguration;  // workspace has one slot per SM
-  cfg.gridDim = dim3((unsigned)(pairs * 2));
-  cfg.stream = s;
   return cudaLaunchKernelEx(&cfg, oz_gemm_tc_pair, ma, mb, P);
 }
 
@@ -1043,18 +1036,18 @@ cudaError_t launch_pair(const CUtensorMap& ma, const CUtensorMap& mb, const Para
 
 cudaError_t ozaki_tc_prepare() {
   if (!tc::encode_fn()) return cudaErrorNotSupported;
-  cudaError_t e = tc::launch_setup<1>().status;
-  if (e == cudaSuccess) e = tc::launch_setup<2>().status;
-  if (e == cudaSuccess) e = tc::launch_setup<4>().status;
-  return e;
+  const tc::DeviceSetup* d = tc::device_setup();
+  return d ? d->status : cudaErrorInvalidDevice;
 }
 
-size_t ozaki_tc_workspace_bytes() { return (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
+// A launch's workspace: a 256-byte header (the wave-pacing counter) and one FP64 accumulator
+// slot of 128 x 256 per CTA.
+size_t ozaki_tc_workspace_bytes() { return tc::WORK_HEADER + (size_t)tc::num_sms() * tc::BM * tc::BN * sizeof(double); }
 size_t ozaki_tc_workspace_bytes_for(int64_t m, int64_t n) {
-  // a launch's grid is at most its tiles, rounded up to whole clusters of up to 4 (and at most one CTA per SM)
+  // a launch's grid is at most one CTA per SM and per tile (the pair form: per 256-row tile, two CTAs)
   const int64_t tiles_m = (m + tc::BM - 1) / tc::BM, tiles_n = (n + tc::BN - 1) / tc::BN;
-  const int64_t ctas = std::min<int64_t>((int64_t)tc::num_sms(), (tiles_m + 3) / 4 * 4 * tiles_n);
-  return (size_t)ctas * tc::BM * tc::BN * sizeof(double);
+  const int64_t ctas = std::min<int64_t>((int64_t)tc::num_sms(), (tiles_m + 1) / 2 * 2 * tiles_n);
+  return tc::WORK_HEADER + (size_t)ctas * tc::BM * tc::BN * sizeof(double);
 }
 int64_t ozaki_tc_pass_blocks() { return tc::PASS_BLOCKS; }
 int ozaki_tc_k_block() { return tc::KB; }
@@ -1084,8 +1077,18 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.first = first_k_tile ? 1 : 0;
   P.C = C;
   P.ldc = ldc;
-  P.work = work;
+  P.pace = (unsigned long long*)work;
+  P.work = (double*)((char*)work + tc::WORK_HEADER);
   P.err = err;
+  P.pace_lag = 0;
+  P.pace_chunk = 16;
+  P.pace_ns = 20000;
+  if (const char* env = getenv("TMM_TC_PACE")) P.pace_lag = atoi(env) < 0 ? 0 : atoi(env);
+  if (const char* env = getenv("TMM_TC_PACE_CHUNK")) {
+    const int c = atoi(env);
+    if (c >= 1 && c <= 4096 && (c & (c - 1)) == 0) P.pace_chunk = c;
+  }
+  if (const char* env = getenv("TMM_TC_PACE_NS")) P.pace_ns = (uint32_t)(atoi(env) < 0 ? 0 : atoi(env));
   P.tiles_n = (int)((n + tc::BN - 1) / tc::BN);
   P.group_m = tc::GROUP_M;
   if (const char* env = getenv("TMM_TC_GROUP_M")) P.group_m = atoi(env) < 1 ? 1 : (atoi(env) > 256 ? 256 : atoi(env));
@@ -1093,35 +1096,27 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   if (const char* env = getenv("TMM_TC_EPI_HINT_NS")) P.epi_hint = (uint32_t)(atoi(env) < 0 ? 0 : atoi(env));
   P.pf = 0;  // measured: any distance (4..32) slows the 8192^3 and 8192^2 x 32768 runs by 30-120 %
   if (const char* env = getenv("TMM_TC_PREFETCH")) P.pf = atoi(env) < 0 ? 0 : (atoi(env) > 64 ? 64 : atoi(env));
-  // Engine form (TMM_TC_CLUSTER overrides): 1, 2, 4 = one-SM MMA on 128 x 256 tiles in
-  // clusters of that many CTAs sharing B by multicast (2 is the default from two row
-  // tiles up); "pair" = CTA-pair MMA on 256 x 256 tiles.  Cycles per k-block and SM,
-  // 11 slices: 8192^3 -> 904 (2), 896 (pair), 893 (1); 16384^3 -> 924 (2), 925 (pair);
-  // 32768^3 -> 966 (2), 1134 (pair).
-  const int64_t tiles128 = (m + tc::BM - 1) / tc::BM;
-  int cm = tiles128 >= 2 ? 2 : 1;  // 0: pair
-  if (const char* env = getenv("TMM_TC_CLUSTER")) {
+  // Engine form: one CTA per SM on 128 x 256 tiles (default), or with TMM_TC_CLUSTER=pair
+  // CTA pairs issuing cta_group::2 MMAs on 256 x 256 tiles.  Cycles per k-block and SM,
+  // 11 slices: 8192^3 -> 893 (one SM), 896 (pair); 16384^3 -> 925 (pair); 32768^3 -> 1134 (pair).
+  int cm = 1;  // 0: pair
+  if (const char* env = getenv("TMM_TC_CLUSTER"))
     if (!strcmp(env, "pair")) cm = 0;
-    const int v = atoi(env);
-    if (v == 1 || v == 2 || v == 4) cm = v;
-  }
   if (cm == 0) {
     if (A.rows_pad % tc::PAIR_M) return cudaErrorInvalidValue;
     P.tiles_m = (int)((m + tc::PAIR_M - 1) / tc::PAIR_M);
     cudaError_t e = tc::make_map(&ma, A, 128);
     if (e == cudaSuccess) e = tc::make_map(&mb, B, 128);
+    if (e == cudaSuccess && P.pace_lag) e = cudaMemsetAsync(P.pace, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     return tc::launch_pair(ma, mb, P, s);
   }
-  P.tiles_m = (int)tiles128;
+  P.tiles_m = (int)((m + tc::BM - 1) / tc::BM);
   cudaError_t e = tc::make_map(&ma, A, tc::BM);
-  if (e == cudaSuccess) e = tc::make_map(&mb, B, tc::BN / cm < OZ_BLOCK ? tc::BN / cm : OZ_BLOCK);
+  if (e == cudaSuccess) e = tc::make_map(&mb, B, OZ_BLOCK);
+  if (e == cudaSuccess && P.pace_lag) e = cudaMemsetAsync(P.pace, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  switch (cm) {
-    case 4: return tc::launch<4>(ma, mb, P, s);
-    case 2: return tc::launch<2>(ma, mb, P, s);
-    default: return tc::launch<1>(ma, mb, P, s);
-  }
+  return tc::launch(ma, mb, P, s);
 }
 
 }  // namespace tmm
