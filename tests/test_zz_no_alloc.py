@@ -48,7 +48,8 @@ def test_no_alloc_matches_regular_entry_twice(tmm):
         st = _noalloc(tmm, ta, tb, m, n, k, alpha, da, lda, db, ldb, beta, c_new, ldc, slices, k_tile,
                       stream.cuda_stream)
         assert st == 0, tmm.lib().tmm_last_error(None)
-        stream.synchronize()
+        # no tensor-core wait gave up on the GPU (the status call waits for the stream)
+        assert tmm.lib().tmm_ozaki_noalloc_status(stream.cuda_stream) == 0, tmm.lib().tmm_last_error(None)
         np.testing.assert_array_equal(c_new.cpu().numpy(), c_ref.cpu().numpy())
         ctx.close()
 
@@ -62,6 +63,16 @@ def test_no_alloc_rejects_oversized_requests(tmm):
                                            128, 0.0, x.data_ptr(), 200000, 20, 0, None)
     assert st == 1
     assert b"scratch" in lib.tmm_last_error(None)
-    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 256, 256, 4096, 1.0, x.data_ptr(), 256, x.data_ptr(), 4096,
-                                           0.0, x.data_ptr(), 256, 13, 1 << 30, None)
-    assert st == 1  # a k_tile beyond what the scratch holds
+    # a k_tile (no larger than k) beyond what the scratch holds for 2048-line operands at 13 slices
+    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 2048, 2048, 8192, 1.0, x.data_ptr(), 2048, x.data_ptr(),
+                                           8192, 0.0, x.data_ptr(), 2048, 13, 8192, None)
+    assert st == 1
+    assert b"k_tile" in lib.tmm_last_error(None)
+    # a k_tile beyond k is an upper bound, not an error: k = 128 with a huge k_tile runs
+    y = torch.ones(256 * 128, dtype=torch.float64, device="cuda")
+    out = torch.zeros(256 * 256, dtype=torch.float64, device="cuda")
+    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 256, 256, 128, 1.0, y.data_ptr(), 256, y.data_ptr(), 128,
+                                           0.0, out.data_ptr(), 256, 4, 1 << 40, None)
+    assert st == 0, lib.tmm_last_error(None)
+    assert lib.tmm_ozaki_noalloc_status(None) == 0
+    assert torch.all(out == 128.0)  # all-ones operands: every entry of C is k

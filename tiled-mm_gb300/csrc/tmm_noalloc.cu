@@ -19,9 +19,14 @@
 //
 // Sharing: every call on every stream of a device uses the same array and the
 // array keeps the last call's contents, so calls that overlap on the GPU race
-// and corrupt each other; serialise them (one stream, or events).  The error
-// word that a timed-out tensor-core wait would set is cleared at the start of
-// each call and is not reported back (the call returns once work is enqueued).
+// and corrupt each other; serialise them (one stream, or events).
+//
+// Errors found on the GPU: the call returns once its work is enqueued, so a
+// tensor-core wait that gives up (after about a second; C is then incomplete)
+// can only be reported later.  It sets an error word in the array that stays
+// set until tmm_ozaki_noalloc_status reads it: that call waits for the given
+// stream, returns TMM_ERROR_TIMEOUT if any call on this device since the last
+// status check gave up (TMM_SUCCESS otherwise) and clears the word.
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress while that device is current (in host code the
@@ -54,6 +59,27 @@ int reject(int status, const std::string& msg) {
   return status;
 }
 
+// The array's device address on the current device (looked up once per device, with
+// that device current: in host code the array's name is a host-side stand-in).
+int scratch_base(const char* who, unsigned char** base) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= MAX_DEVICES)
+    return reject(TMM_ERROR_CUDA, std::string(who) + ": no current CUDA device");
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return reject(TMM_ERROR_CUDA, std::string(who) + ": cudaGetSymbolAddress: " + cudaGetErrorString(e));
+    }
+    g_scratch_ptr[dev] = p;
+  }
+  *base = (unsigned char*)g_scratch_ptr[dev];
+  return TMM_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
@@ -80,7 +106,17 @@ extern "C" int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t
   if (!c || (k > 0 && (!a || !b)))
     return reject(TMM_ERROR_INVALID_ARGUMENT, "tmm_ozaki_gemm_device_noalloc: null matrix pointer");
 
-  // ---- fit the request into the fixed digit region
+  // ---- fit the request into the fixed digit region (m and n are bounded first, so that
+  // the byte counts below cannot overflow: one 128-wide k step of one slice of m + n lines
+  // must fit)
+  if (m > (int64_t)(NOALLOC_DIGIT_BYTES / OZ_K_ALIGN) || n > (int64_t)(NOALLOC_DIGIT_BYTES / OZ_K_ALIGN)) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+             "tmm_ozaki_gemm_device_noalloc: m=%lld, n=%lld: one 128-wide k step needs more digit bytes than the "
+             "fixed %zu-byte scratch holds",
+             (long long)m, (long long)n, NOALLOC_DIGIT_BYTES);
+    return reject(TMM_ERROR_INVALID_ARGUMENT, buf);
+  }
   const int64_t rows_total = oz_round_up(m, OZ_ROW_ALIGN) + oz_round_up(n, OZ_ROW_ALIGN);
   const int64_t per_k = (int64_t)slices * rows_total;  // digit bytes per k element
   const int64_t exp_bytes = 2 * 256 + rows_total * (int64_t)sizeof(int32_t) + 2048;  // exponents + alignment
@@ -93,7 +129,8 @@ extern "C" int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t
              (long long)m, (long long)n, slices, (long long)(per_k * OZ_K_ALIGN + exp_bytes), NOALLOC_DIGIT_BYTES);
     return reject(TMM_ERROR_INVALID_ARGUMENT, buf);
   }
-  int64_t kt = k_tile > 0 ? k_tile : (k < k_room ? k : k_room);
+  // k_tile is an upper bound, as max_tile_k is for the regular entry: a k_tile beyond k is k
+  int64_t kt = k_tile > 0 ? (k_tile < k ? k_tile : k) : (k < k_room ? k : k_room);
   if (kt <= 0) kt = 1;
   if (oz_round_up(kt, OZ_K_ALIGN) > k_room) {
     char buf[256];
@@ -114,26 +151,12 @@ extern "C" int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t
     return reject(TMM_ERROR_NOT_SUPPORTED, "tmm_ozaki_gemm_device_noalloc: device has more SMs than the fixed "
                                            "accumulator slots cover");
   unsigned char* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        cudaGetLastError();
-        return reject(TMM_ERROR_CUDA, std::string("tmm_ozaki_gemm_device_noalloc: cudaGetSymbolAddress: ") +
-                                          cudaGetErrorString(e));
-      }
-      g_scratch_ptr[dev] = p;
-    }
-    base = (unsigned char*)g_scratch_ptr[dev];
-  }
+  if (int st = scratch_base("tmm_ozaki_gemm_device_noalloc", &base)) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  // the error word stays set until tmm_ozaki_noalloc_status reads and clears it
   int* err = (int*)base;
   double* work = (double*)(base + NOALLOC_ERR_BYTES);
   unsigned char* digits = base + NOALLOC_ERR_BYTES + NOALLOC_WORK_BYTES;
-  e = cudaMemsetAsync(err, 0, sizeof(int), s);  // the error word starts at zero
-  if (e != cudaSuccess) return reject(TMM_ERROR_CUDA, "tmm_ozaki_gemm_device_noalloc: clearing the error word failed");
 
   if (k == 0) {
     // C = beta * C with the product empty: one pass of the split-product path is not needed
@@ -154,5 +177,21 @@ extern "C" int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t
     if (e != cudaSuccess)
       return reject(TMM_ERROR_CUDA, std::string("tmm_ozaki_gemm_device_noalloc: launch failed: ") + cudaGetErrorString(e));
   }
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_ozaki_noalloc_status(void* stream) {
+  unsigned char* base = nullptr;
+  if (int st = scratch_base("tmm_ozaki_noalloc_status", &base)) return st;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  int word = 0;
+  // a plain copy of 4 bytes into this stack variable and a 4-byte clear: nothing is allocated
+  if (e == cudaSuccess) e = cudaMemcpy(&word, base, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && word) e = cudaMemset(base, 0, sizeof(int));
+  if (e != cudaSuccess)
+    return reject(TMM_ERROR_CUDA, std::string("tmm_ozaki_noalloc_status: ") + cudaGetErrorString(e));
+  if (word)
+    return reject(TMM_ERROR_TIMEOUT, "tmm_ozaki_noalloc_status: a tensor-core pipeline wait gave up in an earlier "
+                                     "call on this device; its C is incomplete");
   return TMM_SUCCESS;
 }
