@@ -7,16 +7,23 @@ componentwise error metric of both against a twice-working-precision oracle.
 Default workload (--workload ozaki32768): m = n = k = 32768, NN, entries u * 2^e
 with u uniform [-1, 1) and e a uniform integer in [-20, 20] (seeded, synthetic),
 alpha = 1, beta = 0, the slice count the smallest that meets the native path's
-error on a calibration sub-problem of the same k and distribution.
+error on a calibration sub-problem of the same k and distribution; the error at
+6..11 slices on the full problem is reported beside it.
   value    device-resident operands (tmm_gemm_device), CUDA-event timed
   e2e      the public host-pointer call (tmm_gemm) with pinned host buffers:
            every step copies A and B to the device and C back
 Other workloads: native4096 (m = n = k = 4096 NN, uniform, alpha = beta = 1,
-tiles 2048, 2 streams, pinned, copy_c_back).
+tiles 2048, 2 streams, pinned, copy_c_back), the out-of-core, batched, sweep
+and float / complex workloads of the WORKLOADS table.
+
+CPU baselines (rank 0, N = 1): a host dgemm through NumPy's BLAS on all host
+cores (cpu_baseline, on a square sub-block of the workload), and the reference
+algorithm's CPU restatement (the oracle, cpu_baseline_port).
 
 --impl reference times the reference algorithm's CPU restatement (the oracle;
-the reference itself is cuBLAS-backed GPU code that is not present on the GPU
-box) on the host cores, on a bounded k-slab of the same workload.
+the reference itself is cuBLAS-backed GPU code whose sources are not present on
+the GPU machine) on all host cores: every warm-up and timed step is one bounded
+k-slab sample of the same workload.  It imports nothing of this library.
 """
 from __future__ import annotations
 
@@ -35,22 +42,28 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "tiled-mm_gb300"))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
-# measured on this machine's GB300 with the repository's own probes (mma.sync loops, CUDA events)
-# Instruction-rate ceilings on this machine's GB300, measured by tiled-mm_gb300/peaks/engine_rates.cu
-# (dmma, imma; tcgen05 e4m3 M128 N256 K32 back to back from shared memory) and the vendor library's
-# dense e4m3 GEMM (tiled-mm_gb300/peaks/cublaslt_e4m3.py, 8192^3); summarised in
-# profiles/engine_rates.md.
+# Instruction-rate ceilings on this machine's GB300, measured with the repository's own probes
+# (tiled-mm_gb300/peaks/engine_rates.cu: dmma and imma mma.sync loops; tcgen05 e4m3 M128 N256 K32
+# issued back to back from shared memory) and the vendor library's dense e4m3 GEMM
+# (tiled-mm_gb300/peaks/cublaslt_e4m3.py, 8192^3).  The tcgen05 pipe retires 16384 e4m3 FLOP per
+# clock and SM (512 cycles per 128 x 256 x 128 k-block): the tensor roofline of the slice-product
+# kernel is that rate at the SM clock measured during the timed region.
 MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 157.9, "dmma_f64_tflops": 1.099,
                          "tcgen05_e4m3_tflops": 4847.2, "cublaslt_e4m3_tflops": 3948.0}
-# DRAM bytes (read + write) per launch of the slice-product kernel on the device-resident path,
-# from one ncu capture of the workload's own command (profiles/oz_gemm_tc_ozaki32768.md):
-# (workload, launch m, n, k tile, slices) -> bytes
-MEASURED_TRAFFIC = {("ozaki32768", (32768, 32768, 16384), 11): 2.605e12}
+TCGEN05_E4M3_FLOP_PER_CLK_SM = 16384.0
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one slice-product launch, from one
+# ncu capture of a smaller launch with the headline's k tile and slice count (m = n = 8192,
+# k = 16384, 11 slices: the same per-tile sequence, 2048 tiles instead of 32768); a launch of
+# another shape is scaled by its units (tiles x slice pairs x k-blocks), which assumes the
+# traffic per unit does not depend on the number of tiles.  None: no capture for this engine.
+ENGINE_DRAM_CAPTURE = {"launch_mnk": (8192, 8192, 16384), "slices": 11, "bytes": None}
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
-                       path="ozaki", tiles=(16384, 16384, 16384), streams=2,
-                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20], tiles 16384^3"),
+                       path="ozaki", tiles=(16384, 16384, 16384), streams=2, policy="autotune",
+                       e2e_max_tiles=(32768, 32768, 32768),
+                       desc="Ozaki-emulated FP64 GEMM m=n=k=32768 NN, u*2^e, e in [-20,20], k tiles of 16384 "
+                            "on the device, autotuned tiles end to end"),
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
@@ -177,6 +190,144 @@ def measured_peaks() -> dict:
         return json.loads(PEAKS_FILE.read_text())
     except Exception:
         return {}
+
+
+# ----------------------------------------------------------------------------- inputs without the library
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 on uint64 arrays (wrapping arithmetic), the generator's hash."""
+    with np.errstate(over="ignore"):
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def np_generate(kind: int, param: float, seed: int, mat_id: int, rows: int, cols: int, row0: int = 0, col0: int = 0,
+                full_rows: int | None = None) -> np.ndarray:
+    """The rows x cols block at (row0, col0) of the seeded synthetic matrix (column-major, ld = rows),
+    restated in NumPy so that the CPU baselines need nothing of this library: element (i, j) of a
+    full_rows-row matrix hashes seed ^ (id << 56) ^ (i + j * full_rows).  Uniform and u * 2^e entries
+    are bit-identical to the library's generators; the normal kinds agree to rounding."""
+    full_rows = full_rows or rows
+    i = np.arange(row0, row0 + rows, dtype=np.uint64)
+    j = np.arange(col0, col0 + cols, dtype=np.uint64)
+    idx = (i[:, None] + j[None, :] * np.uint64(full_rows)).ravel(order="F")
+    key = np.uint64(seed) ^ (np.uint64(mat_id) << np.uint64(56))
+    h = _splitmix64(idx ^ key)
+    u = (h >> np.uint64(11)).astype(np.float64) * 2.0 ** -52 - 1.0
+    if kind == 0:
+        return u
+    if kind == 2:
+        p = int(param)
+        he = _splitmix64(idx ^ (np.uint64(seed) ^ (np.uint64(mat_id ^ 0x40) << np.uint64(56))))
+        e = (he % np.uint64(2 * p + 1)).astype(np.int64) - p
+        return np.ldexp(u, e.astype(np.int32))
+    if kind in (3, 4):
+        h2 = _splitmix64(idx ^ (np.uint64(seed) ^ (np.uint64(mat_id ^ 0x80) << np.uint64(56))))
+        u1 = 1.0 - (h >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        u2 = (h2 >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        z = np.sqrt(-2.0 * np.log(u1)) * np.cos(np.pi * 2.0 * u2)
+        line = np.broadcast_to(i[:, None] if kind == 3 else j[None, :], (rows, cols))
+        hf = _splitmix64(line.ravel(order="F") ^ (np.uint64(seed) ^ (np.uint64(mat_id ^ 0x40) << np.uint64(56))))
+        f = (2.0 * (hf >> np.uint64(11)).astype(np.float64) * 2.0 ** -53 - 1.0) * param
+        return z * np.exp2(f)
+    raise ValueError(f"generator kind {kind} is not restated here")
+
+
+def host_blas_info() -> str:
+    try:
+        cfg = np.show_config(mode="dicts")
+        blas = cfg.get("Build Dependencies", {}).get("blas", {})
+        return f"{blas.get('name', 'unknown')} {blas.get('version', '')}".strip()
+    except Exception:
+        return "unknown"
+
+
+def host_blas_baseline(w, seconds_budget: float = 12.0) -> dict:
+    """A host dgemm (NumPy's BLAS, all host cores) on a square sub-block of the workload's own
+    matrices: the leading min(m, n, k, 8192)^3 product of A and B, timed until the budget."""
+    cores = len(os.sched_getaffinity(0))
+    d = min(w["m"], w["n"], w["k"], 8192)
+    a = np_generate(w["kind"], w["param"], 0, 0, d, d, full_rows=w["m"]).reshape(d, d, order="F")
+    b = np_generate(w["kind"], w["param"], 0, 1, d, d, full_rows=w["k"]).reshape(d, d, order="F")
+    c = a @ b  # warm-up (BLAS threads start)
+    reps, t = 0, 0.0
+    t0 = time.perf_counter()
+    while t < seconds_budget / 2 or reps < 2:
+        np.matmul(a, b, out=c)
+        reps += 1
+        t = time.perf_counter() - t0
+        if reps >= 50:
+            break
+    return {"value": 2.0 * d ** 3 * reps / t / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "host_blas",
+            "blas": host_blas_info(), "sample": f"dgemm {d}x{d}x{d} (the leading block of the workload's A and B), "
+            f"{reps} calls in {t:.1f} s", "seconds": t / reps}
+
+
+def oracle_sample_setup(w, seconds_target: float):
+    """The oracle (the reference algorithm restated on the CPU: tiled GEMM with the reference's
+    tile semantics, per-tile plain product) and a k-slab of the workload (full m and n) sized so
+    that one sample takes about seconds_target on all host threads.  Inputs come from the NumPy
+    restatement of the generator: nothing of this library is loaded."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import load_oracle, oracle_gemm
+
+    oracle = load_oracle()
+    cores = len(os.sched_getaffinity(0))
+    m, n = w["m"], w["n"]
+    c = np.zeros(m * n)
+
+    def make(k):
+        a = np_generate(w["kind"], w["param"], 0, 0, m, k, full_rows=m)
+        b = np_generate(w["kind"], w["param"], 0, 1, k, n, full_rows=w["k"])
+        return a, b
+
+    def sample(a, b, k):
+        t0 = time.perf_counter()
+        oracle_gemm(oracle, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m, (min(m, 4096), min(n, 4096), k),
+                    nthreads=cores)
+        return time.perf_counter() - t0
+
+    k = 8
+    a, b = make(k)
+    dt = sample(a, b, k)
+    k = int(min(w["k"], max(8, k * seconds_target / max(dt, 1e-3))))
+    a, b = make(k)
+    return (lambda: sample(a, b, k)), m, n, k, cores
+
+
+def cpu_baseline_port(w, seconds_budget: float = 15.0) -> dict:
+    """The oracle port on a k-slab of the workload, all host threads (kind "port")."""
+    run, m, n, k, cores = oracle_sample_setup(w, seconds_budget / 2)
+    times = [run() for _ in range(2)]
+    dt = min(times)
+    return {"value": 2.0 * m * n * k / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"k-slab m={m} n={n} k={k} of the workload ({dt:.1f} s)", "seconds": dt}
+
+
+def host_link_bandwidth(torch, nbytes: int = 1 << 30) -> dict:
+    """Pinned host <-> device copy bandwidth (GB/s), best of 3, CUDA events: the link term of the
+    end-to-end roofline."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, fn in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+        best = None
+        for _ in range(3):
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        out[name] = nbytes / best / 1e9
+    del h, d
+    return out
 
 
 # ----------------------------------------------------------------------------- our implementation
@@ -308,6 +459,28 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
                               n_samples=args.samples, seed=11)
     result["error_metric"] = e_ours
 
+    # ---- the error at each slice count on the full problem (one untimed-for-the-value call each,
+    # event-timed for reference), beside the native path's error below
+    if w["path"] == "ozaki" and args.sweep_slices:
+        c_pin = torch.empty(m * n, dtype=torch.float64).pin_memory()
+        sweep = {}
+        for s_try in [int(x) for x in args.sweep_slices.split(",")]:
+            ctx.set_path(tmm.PATH_OZAKI, s_try)
+            Cd.copy_(C0)
+            ev[0].record(stream)
+            dev_step()
+            ev[1].record(stream)
+            ev[1].synchronize()
+            t_s = ev[0].elapsed_time(ev[1]) / 1e3
+            c_pin.copy_(Cd)
+            e_s = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m,
+                                   c_pin.numpy(), m, n_samples=args.samples, seed=11)
+            sweep[s_try] = {"error_metric": e_s, "tflops": flops / t_s / 1e12, "slice_pairs": s_try * (s_try + 1) // 2}
+            log(f"full-size sweep: slices={s_try} metric={e_s:.3e} {flops / t_s / 1e12:.1f} TFLOP/s")
+        ctx.set_path(tmm.PATH_OZAKI, slices)
+        result["slice_sweep_full_size"] = sweep
+        del c_pin
+
     # ---- native path on the same device-resident inputs (for the "vs native" comparison)
     if w["path"] == "ozaki" and not args.skip_native:
         nctx = tmm.make_context(np.float64, 1, *w["tiles"])
@@ -343,8 +516,9 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     c_init = hc.copy() if w["beta"] != 0 else None
     del A, B, Cd
     torch.cuda.empty_cache()
-    hctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
-    if w.get("policy") == "autotune":
+    hctx = tmm.make_context(np.float64, w["streams"], *w.get("e2e_max_tiles", w["tiles"]))
+    autotune = w.get("policy") == "autotune" and not args.tiles
+    if autotune:
         hctx.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
     if slices:
         hctx.set_path(tmm.PATH_OZAKI, slices)
@@ -356,10 +530,13 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], hc, m,
                  pin_host_buffers=w.get("pin", False), copy_c_back=copy_back)
 
-    for _ in range(max(1, args.e2e_warmup)):
+    # warm-up; with the autotuner, until it has timed its candidates (each warm-up call runs one)
+    for i in range(max(1, args.e2e_warmup) + (8 if autotune else 0)):
         if c_init is not None:
             hc[:] = c_init
         e2e_call()
+        if i + 1 >= max(1, args.e2e_warmup) and (not autotune or hctx.stats()["autotune_state"] >= 2):
+            break
     hctx.set_kernel_timing(True)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as e2e_clk:
         for _ in range(args.e2e_steps):
@@ -369,6 +546,7 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             e2e_call()
             e2e_times.append(time.perf_counter() - t0)
     e2e_kernel_s, _ = hctx.kernel_time()
+    e2e_busy_s, e2e_span_s = hctx.kernel_busy_time()
     hctx.set_kernel_timing(False)
     st = hctx.stats()
     t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
@@ -380,10 +558,15 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
                      if pageable else "pinned (cudaHostAlloc)",
                      "copy_c_back": copy_back, "steps": args.e2e_steps,
                      "step_seconds": [round(x, 4) for x in e2e_times],
-                     "engine_kernel_seconds_per_step": e2e_kernel_s / max(1, args.e2e_steps),
+                     # the union of the engine launches' device intervals (launches on the two
+                     # compute streams overlap) and their sum, per step
+                     "engine_busy_seconds_per_step": e2e_busy_s / max(1, args.e2e_steps),
+                     "engine_launch_seconds_sum_per_step": e2e_kernel_s / max(1, args.e2e_steps),
                      "clocks": e2e_clk.summary()}
     result["e2e"]["direct_bytes_per_step"] = st["direct_bytes"]
     result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"], st["n_streams"]]
+    if autotune:
+        result["e2e"]["autotune"] = {"state": st["autotune_state"], "report": hctx.autotune_report()}
     result["e2e_tiles_loaded"] = st["tiles_loaded"]
     hctx.close()
     ctx.close()
@@ -393,18 +576,30 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     if w["path"] == "ozaki":
         pairs = slices * (slices + 1) // 2
         lowp_ops = pairs * flops
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        max_mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+
+        def pipe_peak(clocks: dict) -> tuple[float, float]:
+            mhz = (clocks or {}).get("sm_mhz") or max_mhz
+            return TCGEN05_E4M3_FLOP_PER_CLK_SM * sms * mhz * 1e6 / 1e12, mhz
+
         if eng["engine"] == "imma":
-            peak = MEASURED_ENGINE_PEAKS["imma_s8_tops"]
-            src = "mma.sync m16n8k32 s8 issue rate, tiled-mm_gb300/peaks/engine_rates.cu"
+            peak, mhz = MEASURED_ENGINE_PEAKS["imma_s8_tops"], None
+            src = "mma.sync m16n8k32 s8 issue rate measured on this GPU (engine_rates probe)"
         else:
-            bf16 = measured_peaks().get("bf16_tflops") or 1910.1
-            peak = 2.0 * bf16
-            src = "2 x the measured dense bf16 cuBLAS burst rate in MEASURED_PEAKS.json (e4m3 issues at twice bf16)"
+            peak, mhz = pipe_peak(result["clocks"])
+            src = (f"tcgen05.mma kind::f8f6f4 pipe rate, {TCGEN05_E4M3_FLOP_PER_CLK_SM:.0f} FLOP/clk/SM (measured "
+                   f"back to back on this GPU) x {sms} SMs x the median SM clock of the timed region ({mhz:.0f} MHz)")
         # algorithmic low-precision operations per launch over the average launch duration
         achieved = lowp_ops * args.steps / kernel_seconds / 1e12
         # the device-resident path launches the engine on all of C per k tile
         launch = (m, n, min(k, w["tiles"][2]))
-        traffic = MEASURED_TRAFFIC.get((args.workload, launch, slices))
+        traffic = None
+        cap = ENGINE_DRAM_CAPTURE
+        if eng["engine"] == "tcgen05" and cap["bytes"]:
+            def units(mm, nn, kk, s_):
+                return -(-mm // 128) * -(-nn // 256) * (s_ * (s_ + 1) // 2) * -(-kk // 128)
+            traffic = cap["bytes"] * units(*launch, slices) / units(*cap["launch_mnk"], cap["slices"])
         result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": traffic,
                               "kernel": "oz_gemm_tc" if eng["engine"] == "tcgen05" else "oz_gemm_imma",
@@ -412,13 +607,33 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
                               "ops": f"{pairs} slice-pair products x 2mnk per step, over the engine launches' "
                                      "event-timed durations",
                               "peak_source": src}
+        if traffic:
+            algo = slices * (launch[0] + launch[1]) * launch[2] + 8 * launch[0] * launch[1]
+            result["roofline"]["traffic_source"] = (
+                f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch m={cap['launch_mnk'][0]} "
+                f"n={cap['launch_mnk'][1]} k={cap['launch_mnk'][2]} at {cap['slices']} slices, scaled by tiles x "
+                f"pairs x k-blocks")
+            result["roofline"]["algorithmic_bytes_per_launch"] = algo
+            result["roofline"]["traffic_over_algorithmic"] = traffic / algo
         if eng["engine"] == "tcgen05":
+            bf16 = measured_peaks().get("bf16_tflops") or 1910.1
             result["roofline"]["frac_of_other_ceilings"] = {
                 "cublaslt_e4m3_gemm": achieved / MEASURED_ENGINE_PEAKS["cublaslt_e4m3_tflops"],
-                "tcgen05_pipe_back_to_back": achieved / MEASURED_ENGINE_PEAKS["tcgen05_e4m3_tflops"]}
-        if traffic:
-            result["roofline"]["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " \
-                                                   "profiles/oz_gemm_tc_ozaki32768.md"
+                "two_x_bf16_burst": achieved / (2.0 * bf16),
+                "tcgen05_pipe_at_max_clock": achieved / pipe_peak({"sm_mhz": max_mhz})[0]}
+            # spec roofline of the host-pointer call: the slower of the slice products at the
+            # pipe rate (at the e2e run's clock) and the host-link traffic at the measured bandwidth
+            link = host_link_bandwidth(torch)
+            p_e2e, mhz_e2e = pipe_peak(result["e2e"]["clocks"])
+            t_compute = lowp_ops / (p_e2e * 1e12)
+            t_h2d = result["e2e"]["h2d_bytes_per_step"] / (link["h2d_gbs"] * 1e9)
+            t_d2h = result["e2e"]["d2h_bytes_per_step"] / (link["d2h_gbs"] * 1e9)
+            t_roof = max(t_compute, t_h2d, t_d2h)
+            result["e2e"]["roofline"] = {
+                "t_roof_seconds": t_roof, "t_measured_seconds": result["e2e"]["seconds_per_step"],
+                "frac": t_roof / result["e2e"]["seconds_per_step"],
+                "terms_seconds": {"compute": t_compute, "h2d": t_h2d, "d2h": t_d2h},
+                "link_gbs": link, "pipe_tflops_at_clock": p_e2e, "sm_mhz": mhz_e2e}
         result["slices"] = slices
         result["slice_pairs"] = pairs
         result["engine"] = eng
@@ -429,7 +644,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         achieved = flops * args.steps / kernel_seconds / 1e12
         result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": None, "kernel": "gemm_f64_dmma",
-                              "peak_source": "mma.sync m16n8k4 f64 issue rate, tiled-mm_gb300/peaks/engine_rates.cu"}
+                              "peak_source": "mma.sync m16n8k4 f64 issue rate measured on this GPU (engine_rates "
+                                             "probe)"}
     return result
 
 
@@ -700,33 +916,23 @@ def run_embedded(args, w, rank, world, dist, log) -> dict:
             "e2e": None, "gpu_launches": None}
 
 
-def cpu_baseline(w, seconds_budget: float = 20.0) -> dict:
-    """The reference algorithm's CPU restatement (the oracle: tiled GEMM with the reference's tile
-    semantics, per-tile plain GEMM) on a k-slab of the workload, all host threads."""
-    sys.path.insert(0, str(ROOT / "tests"))
-    from oracle_lib import load_oracle, oracle_gemm
-
-    import tiledmm as tmm
-
-    oracle = load_oracle()
-    cores = len(os.sched_getaffinity(0))
-    m, n = w["m"], w["n"]
-    k = 64
-    while True:
-        a = np.zeros(m * k)
-        b = np.zeros(k * n)
-        tmm.fill_host(a, m, k, m, w["kind"], w["param"], seed=0, mat_id=0)
-        tmm.fill_host(b, k, n, k, w["kind"], w["param"], seed=0, mat_id=1)
-        c = np.zeros(m * n)
-        t0 = time.perf_counter()
-        oracle_gemm(oracle, "N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m, (min(m, 4096), min(n, 4096), k),
-                    nthreads=cores)
-        dt = time.perf_counter() - t0
-        if dt * 4 > seconds_budget or k >= w["k"]:
-            break
-        k = min(w["k"], k * 4)
-    return {"value": 2.0 * m * n * k / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-            "sample": f"k-slab m={m} n={n} k={k} of the workload ({dt:.1f} s)", "seconds": dt}
+def run_reference_arm(args, w, base: dict) -> dict:
+    """The reference algorithm's CPU restatement on all host threads: each warm-up and timed step
+    is one k-slab sample of the workload (full m and n), sized for about a second and a half, so
+    that the whole run ends within a few minutes."""
+    run, m, n, k, cores = oracle_sample_setup(w, 1.5)
+    for _ in range(args.warmup):
+        run()
+    times = [run() for _ in range(args.steps)]
+    t = float(np.mean(times))
+    value = 2.0 * m * n * k / t / 1e12
+    sample = f"k-slab m={m} n={n} k={k} of the workload per step"
+    return dict(base, impl="reference", value=value, ms_per_step=t * 1e3,
+                cpu_baseline={"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
+                e2e={"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                reference_note="the reference's per-tile arithmetic is cuBLAS on a GPU and its sources are not on "
+                               "the GPU machine; its algorithm (tiled GEMM, the reference's tile semantics) is timed "
+                               "as the oracle's CPU restatement on the host cores, one k-slab sample per step")
 
 
 def main() -> None:
@@ -749,6 +955,8 @@ def main() -> None:
     ap.add_argument("--pin", default="workload", choices=["workload", "on", "off"],
                     help="pin_host_buffers of the end-to-end call (default: the workload's)")
     ap.add_argument("--sweep-sizes", default="4000,6000,8000,10000,12000,14000,16000,18000,20000")
+    ap.add_argument("--sweep-slices", default="6,7,8,9,10,11",
+                    help="slice counts whose error is measured on the full problem (empty: none)")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload], engine=args.engine)
     if args.tiles:
@@ -768,13 +976,7 @@ def main() -> None:
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(w)
-        line = dict(base, impl="reference", value=cb["value"], ms_per_step=cb["seconds"] * 1e3,
-                    cpu_baseline=cb, e2e={"value": cb["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
-                                          "d2h_bytes_per_step": 0})
-        line["config"] = dict(config, reference_note="the reference's per-tile arithmetic is cuBLAS on a GPU; "
-                              "its algorithm is timed here as the oracle's CPU restatement on the host cores")
-        print(json.dumps(line), flush=True)
+        print(json.dumps(run_reference_arm(args, w, base)), flush=True)
         return
 
     if w["path"] == "embedded":
@@ -817,8 +1019,9 @@ def main() -> None:
     if rank == 0:
         line = dict(base)
         line.update(res)
-        if not args.skip_cpu:
-            line["cpu_baseline"] = cpu_baseline(w)
+        if not args.skip_cpu and world == 1:
+            line["cpu_baseline"] = host_blas_baseline(w)
+            line["cpu_baseline_port"] = cpu_baseline_port(w)
         peaks = measured_peaks()
         if peaks:
             line["measured_peaks_file"] = {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops", "bf16_tflops_sustained")}

@@ -6,9 +6,10 @@ the host stand-in for the CUDA runtime and cuBLAS (oracle/fake_cuda, recipe in
 oracle/Makefile) and run on the known-answer inputs of its own test
 (tests/test-multiply.cpp:58-66: std::mt19937(42), integers 0..9, drawn A, B,
 C) at the shapes its CI and ctest use.  Needs the reference sources
-(TMM_REFERENCE_DIR, default /root/reference) and g++; run from the repo root:
+(the environment variable TMM_REFERENCE_DIR names the checkout; required) and
+g++; run from the repo root:
 
-    python tests/golden/make_golden.py
+    TMM_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -51,7 +52,7 @@ def kat_inputs(na: int, nb: int, nc: int) -> tuple[np.ndarray, np.ndarray, np.nd
 def main() -> None:
     ref = load_ref_host()
     if ref is None:
-        raise SystemExit("reference sources not found")
+        raise SystemExit("reference sources not found: set TMM_REFERENCE_DIR to the reference checkout")
     out: dict[str, np.ndarray] = {}
     for (name, m, n, k, tr, tm, tn, tk, streams, alpha, beta, pad) in CASES:
         ta, tb = tr[0], tr[1]

@@ -14,7 +14,9 @@ ROOT = Path(__file__).resolve().parents[1]
 ORACLE = ROOT / "oracle"
 ORACLE_SO = ORACLE / "_build" / "libtmm_oracle.so"
 REF_SO = ORACLE / "_ref" / "libtiledmm_ref_host.so"
-REFERENCE_DIR = Path(os.environ.get("TMM_REFERENCE_DIR", "/root/reference"))
+# the reference checkout, where one exists (set by the build step that compiles oracle/_ref)
+_REF_ENV = os.environ.get("TMM_REFERENCE_DIR", "")
+REFERENCE_DIR = Path(_REF_ENV) if _REF_ENV else None
 
 _p, _i64, _ci, _d = C.c_void_p, C.c_int64, C.c_int, C.c_double
 DT = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.complex64): 2, np.dtype(np.complex128): 3}
@@ -55,9 +57,8 @@ def load_oracle() -> C.CDLL:
 def load_ref_host() -> C.CDLL | None:
     """The reference's host code (tile policy, geometry, schedule) compiled from its own sources
     against oracle/fake_cuda; None where the reference sources are absent."""
-    src = REFERENCE_DIR / "src" / "Tiled-MM" / "tiled_mm.cpp"
     if not REF_SO.exists():
-        if not src.exists():
+        if REFERENCE_DIR is None or not (REFERENCE_DIR / "src" / "Tiled-MM" / "tiled_mm.cpp").exists():
             return None
         _make("ref")
     try:

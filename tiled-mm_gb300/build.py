@@ -4,9 +4,7 @@
 
 Every translation unit is compiled by nvcc for sm_103a only, in parallel, then
 linked into one shared library with the CUDA runtime linked statically (the
-library needs no LD_LIBRARY_PATH and no cuBLAS).  A second, optional library,
-libtmm_cublas_cmp.so, wraps cuBLAS for the comparison runs in bench.py only; it
-is never linked into or loaded by the product library.
+library needs no LD_LIBRARY_PATH and no cuBLAS).
 """
 from __future__ import annotations
 
@@ -26,9 +24,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", str(PKG.parent / "include"), "-I", str(CSRC)]
 
 SOURCES = ["tmm_core.cpp", "tmm_native.cu", "tmm_ozaki.cu", "tmm_tcgen05.cu", "tmm_batched.cu", "tmm_autotune.cpp",
-           "tmm_noalloc.cu", "tmm_xt.cpp", "tmm_ozaki_embed.cu"]
+           "tmm_noalloc.cu", "tmm_xt.cpp", "tmm_ozaki_embed.cu", "tmm_dropin.cpp"]
 LIB = OUT / "libtiledmm_gb300.so"
-CMP_LIB = OUT / "libtmm_cublas_cmp.so"
 
 
 def _run(cmd: list[str]) -> None:
@@ -63,11 +60,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
     if force or jobs or not LIB.exists():
-        _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", str(LIB), *map(str, objs), "-lpthread", "-ldl", "-lrt"])
-    cmp_src = CSRC / "cublas_cmp.cpp"
-    if cmp_src.exists() and (force or not _newer(CMP_LIB, [cmp_src])):
-        _run([NVCC, *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(cmp_src), "-o", str(CMP_LIB),
-              "-lcublas", "-Xlinker", "-rpath=/usr/local/cuda/lib64"])
+        _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-Xlinker", f"-soname={LIB.name}", "-o", str(LIB),
+              *map(str, objs), "-lpthread", "-ldl", "-lrt"])
     if verbose:
         print(f"built {LIB}")
     return LIB
