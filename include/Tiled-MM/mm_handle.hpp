@@ -26,15 +26,20 @@ class mm_handle {
  public:
   // creates the streams; device memory is sized lazily by the first gemm (mm_handle.cpp:11-29)
   mm_handle(int streams, int max_tile_m, int max_tile_n, int max_tile_k)
-      : ctx_(create(streams, max_tile_m, max_tile_n, max_tile_k)), gpu_ctx_(ctx_), a_buff_(streams),
-        b_buff_(streams), c_buff_(streams) {}
+      : ctx_(create(streams, max_tile_m, max_tile_n, max_tile_k)), gpu_ctx_(ctx_), a_buff_(ctx_, 'a', streams),
+        b_buff_(ctx_, 'b', streams), c_buff_(ctx_, 'c', streams) {}
   ~mm_handle() { tmm_destroy(ctx_); }
 
   mm_handle(mm_handle&&) = delete;
   mm_handle(const mm_handle&) = delete;
   mm_handle& operator=(const mm_handle&& other) = delete;
 
-  void set_num_streams(int streams) { check_tmm_status(tmm_set_num_streams(ctx_, streams), ctx_); }
+  void set_num_streams(int streams) {
+    gpu_ctx_.set_num_streams(streams);
+    a_buff_.set_num_streams(streams);
+    b_buff_.set_num_streams(streams);
+    c_buff_.set_num_streams(streams);
+  }
   int get_num_streams() {
     int n = 0;
     check_tmm_status(tmm_get_num_streams(ctx_, &n), ctx_);
@@ -63,6 +68,9 @@ class mm_handle {
   }
   void set_streams_and_tiles(int streams, int tile_m, int tile_n, int tile_k) {
     check_tmm_status(tmm_set_streams_and_tiles(ctx_, streams, tile_m, tile_n, tile_k), ctx_);
+    a_buff_.set_num_streams(streams);
+    b_buff_.set_num_streams(streams);
+    c_buff_.set_num_streams(streams);
     sync_tiles();
   }
 

@@ -1,9 +1,15 @@
 // Drop-in for src/Tiled-MM/tiled_mm.hpp of eth-cscs/Tiled-MM:
 //   C = alpha * op(A) * op(B) + beta * C from host pointers, column-major,
 //   op in {N, T, C}, on one GPU (tiled_mm.hpp:69-79).
-// Same signature and default arguments; the work is done by the GB300
-// library through the C ABI (include/tmm_c_api.h).  Sizes are 64-bit inside.
+// Same declaration and default arguments.  As in the reference, the template is
+// defined in the compiled library, which carries its explicit instantiations
+// for float, double, std::complex<float> and std::complex<double>
+// (tiled_mm.cpp:626-668); link with libtiledmm_gb300 (CMake: the imported target
+// Tiled-MM::Tiled-MM of find_package(Tiled-MM)).  The work is done by the GB300
+// kernels behind the C ABI (include/tmm_c_api.h); sizes are 64-bit inside.
 #pragma once
+#include <complex>
+
 #include "mm_handle.hpp"
 
 namespace gpu {
@@ -11,11 +17,18 @@ namespace gpu {
 template <typename Scalar>
 void gemm(mm_handle<Scalar>& handle, char trans_a, char trans_b, int m, int n, int k, Scalar alpha, Scalar* a,
           int ld_a, Scalar* b, int ld_b, Scalar beta, Scalar* c, int ld_c, bool pin_host_buffers = true,
-          bool copy_c_back = true) {
-  int st = tmm_gemm(handle.native(), trans_a, trans_b, m, n, k, &alpha, a, ld_a, b, ld_b, &beta, c, ld_c,
-                    pin_host_buffers ? 1 : 0, copy_c_back ? 1 : 0);
-  check_tmm_status(st, handle.native());
-  handle.after_gemm();
-}
+          bool copy_c_back = true);
+
+extern template void gemm<float>(mm_handle<float>&, char, char, int, int, int, float, float*, int, float*, int, float,
+                                 float*, int, bool, bool);
+extern template void gemm<double>(mm_handle<double>&, char, char, int, int, int, double, double*, int, double*, int,
+                                  double, double*, int, bool, bool);
+extern template void gemm<std::complex<float>>(mm_handle<std::complex<float>>&, char, char, int, int, int,
+                                               std::complex<float>, std::complex<float>*, int, std::complex<float>*,
+                                               int, std::complex<float>, std::complex<float>*, int, bool, bool);
+extern template void gemm<std::complex<double>>(mm_handle<std::complex<double>>&, char, char, int, int, int,
+                                                std::complex<double>, std::complex<double>*, int,
+                                                std::complex<double>*, int, std::complex<double>,
+                                                std::complex<double>*, int, bool, bool);
 
 }  // namespace gpu

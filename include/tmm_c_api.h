@@ -122,11 +122,21 @@ int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int
  * GPU race.  The first call on a device looks up the array's device address;
  * make it before any stream capture.  Enqueues on `stream` (NULL: legacy
  * default stream) and returns; results equal tmm_gemm_device's with the
- * tcgen05 engine, the same slice count and max_tile_k = k_tile. */
+ * tcgen05 engine, the same slice count and max_tile_k = k_tile (k_tile is an
+ * upper bound: a k_tile beyond k means one k step).  A tensor-core wait that
+ * gives up on the GPU (after about a second; C is then incomplete) is
+ * reported by tmm_ozaki_noalloc_status, not by this call. */
 int tmm_ozaki_gemm_device_noalloc(char trans_a, char trans_b, int64_t m, int64_t n, int64_t k, double alpha,
                                   const double* a_dev, int64_t ld_a, const double* b_dev, int64_t ld_b,
                                   double beta, double* c_dev, int64_t ld_c, int slices, int64_t k_tile,
                                   void* stream);
+
+/* No counterpart in the reference.  Device-side status of the allocation-free
+ * entry above: waits for `stream` (a cudaStream_t; NULL: legacy default
+ * stream), then returns TMM_ERROR_TIMEOUT if a call on the current device gave
+ * up waiting inside the tensor-core pipeline since the last status check, and
+ * TMM_SUCCESS otherwise; clears the word it read.  Allocates nothing. */
+int tmm_ozaki_noalloc_status(void* stream);
 
 /* One problem of a batch (tmm_gemm_batched). */
 typedef struct tmm_batch_problem {
@@ -157,6 +167,34 @@ int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_problem* probl
  * and its device_vector::data()/size()/capacity() (src/Tiled-MM/device_vector.hpp:67-80):
  * the device pointer of the compact (ld = m) result left by copy_c_back == 0. */
 int tmm_get_full_c(tmm_context* ctx, void** device_ptr, size_t* size_elems, size_t* capacity_elems);
+
+/* ------------------------------------------------------------------ streams, events, device buffers */
+
+/* gpu_context::get_stream(stream_id) (src/Tiled-MM/gpu_context.cpp:27-32): the context's
+ * compute stream stream_id (a cudaStream_t), 0 <= stream_id < the stream count; out of range
+ * gives TMM_ERROR_INVALID_ARGUMENT. */
+int tmm_get_stream(tmm_context* ctx, int stream_id, void** stream);
+/* gpu_context::get_result_stream() (src/Tiled-MM/gpu_context.cpp:55-57): the stream results
+ * return to the host on. */
+int tmm_get_result_stream(tmm_context* ctx, void** stream);
+/* device_buffer::data() / stream_buffer(stream_id) of the handle's A, B or C buffer
+ * (src/Tiled-MM/device_buffer.hpp:19-21, 49-63): which is 'a', 'b' or 'c'; stream_id -1 gives
+ * the buffer's base.  C: the first result-tile slot of compute stream stream_id.  A and B: this
+ * library caches device tiles instead of keeping one slot per stream, so the pointer is that of
+ * cache slot stream_id.  NULL until the first gemm has sized the buffers. */
+int tmm_get_device_buffer(tmm_context* ctx, char which, int stream_id, void** ptr);
+
+/* device_stream / device_event (src/Tiled-MM/device_stream.hpp:8-75,
+ * src/Tiled-MM/device_event.hpp:9-80) over the current device: a non-blocking stream, an event
+ * (timing enabled, so that time_since works), recording, host and stream waits, elapsed seconds. */
+int tmm_stream_create(void** stream);
+int tmm_stream_destroy(void* stream);
+int tmm_event_create(void** event);
+int tmm_event_destroy(void* event);
+int tmm_event_record(void* event, void* stream);
+int tmm_event_synchronize(void* event);
+int tmm_event_elapsed(void* start, void* end, double* seconds);
+int tmm_stream_wait_event(void* stream, void* event);
 
 /* ------------------------------------------------------------------ handle settings */
 
@@ -202,8 +240,17 @@ enum tmm_ozaki_engine { TMM_OZAKI_IMMA = 0, TMM_OZAKI_TCGEN05 = 1 };
 int tmm_set_ozaki_engine(tmm_context* ctx, int engine);
 int tmm_get_ozaki_engine(tmm_context* ctx, int* engine, int* k_block, int64_t* pass_blocks);
 
-/* New: tile policy (enum tmm_tile_policy). */
+/* New: tile policy (enum tmm_tile_policy).  TMM_TILE_POLICY_AUTOTUNE times a few candidate
+ * tile sets (sizes that fit the device memory, k tiles halved and quartered, m and n tiles
+ * halved) per size class -- dtype, path, engine, slices, log2 of m, n and k, trans, pinning,
+ * copy-back -- over the first calls of the class (each call computes the whole product with
+ * one candidate), then uses the fastest; TMM_AUTOTUNE_CACHE names a file that keeps the
+ * choices across processes.  It replaces the reference's divisor rule
+ * (src/Tiled-MM/mm_handle.cpp:89-133), which stays the default policy. */
 int tmm_set_tile_policy(tmm_context* ctx, int policy);
+/* New: the autotuner's measurements for the size class of this context's last autotuned call
+ * (candidates, their FP64-equivalent TFLOP/s, the chosen one), as text into text[capacity]. */
+int tmm_get_autotune_report(tmm_context* ctx, char* text, size_t capacity);
 
 /* New: cap on the device memory the context may hold (0 = no cap beyond what
  * is free on the device).  Smaller caps force out-of-core tiling. */
@@ -225,6 +272,9 @@ typedef struct tmm_stats {
                              the host page tables: unregistered host tiles are copied by kernel */
   uint64_t direct_bytes;  /* bytes of the last call copied by kernel between unregistered host memory and
                              the device (the rest of h2d_bytes / d2h_bytes went through the copy engines) */
+  int autotune_state;     /* TMM_TILE_POLICY_AUTOTUNE: 1 the call ran an untimed candidate of its size class,
+                             2 the fastest measured candidate, 3 a choice read from TMM_AUTOTUNE_CACHE;
+                             0 another policy */
 } tmm_stats;
 
 int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);
@@ -236,6 +286,10 @@ int tmm_get_stats(tmm_context* ctx, tmm_stats* stats);
  * launches and returns the summed device time (seconds) and the number of launches. */
 int tmm_set_kernel_timing(tmm_context* ctx, int on);
 int tmm_get_kernel_time(tmm_context* ctx, double* seconds, uint64_t* launches);
+/* The same launches as device busy time: the length of the union of their [start, end]
+ * intervals (launches on several streams that overlap count once) and the span from the
+ * first start to the last end, in seconds, since timing was switched on. */
+int tmm_get_kernel_busy_time(tmm_context* ctx, double* busy_seconds, double* span_seconds);
 
 /* Message of the last failure of this context (ctx == NULL: of the calling
  * thread's last context-free call).  Never NULL. */

@@ -130,3 +130,56 @@ def test_c_header_is_plain_c(tmp_path):
 def test_cpp_dropin_headers_compile():
     subprocess.run(["g++", "-std=c++14", "-Wall", "-fsyntax-only", "-I", str(ROOT / "include"),
                     str(ROOT / "tests" / "cpp" / "test_multiply_gb300.cpp")], check=True)
+
+
+def test_noalloc_argument_checks_need_no_gpu(tmm):
+    """The allocation-free entry rejects bad arguments and oversized requests before it
+    touches a device (the pointers below are never dereferenced)."""
+    lib = tmm.lib()
+    fake = 256  # a non-null stand-in pointer
+    assert lib.tmm_ozaki_gemm_device_noalloc(b"X", b"N", 8, 8, 8, 1.0, fake, 8, fake, 8, 0.0, fake, 8, 4, 0, None) == 1
+    assert lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 8, 8, 8, 1.0, fake, 8, fake, 8, 0.0, fake, 8, 0, 0, None) == 1
+    # m near 2^62: rejected before any byte count could overflow
+    big = 1 << 62
+    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", big, 8, 128, 1.0, fake, big, fake, 128, 0.0, fake, big, 4, 0,
+                                           None)
+    assert st == 1 and b"scratch" in lib.tmm_last_error(None)
+    # 20 slices of two 200000-line operands cannot fit one 128-wide k step
+    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 200000, 200000, 128, 1.0, fake, 200000, fake, 128, 0.0, fake,
+                                           200000, 20, 0, None)
+    assert st == 1 and b"scratch" in lib.tmm_last_error(None)
+    # a k_tile no larger than k that the scratch cannot hold
+    st = lib.tmm_ozaki_gemm_device_noalloc(b"N", b"N", 2048, 2048, 8192, 1.0, fake, 2048, fake, 8192, 0.0, fake, 2048,
+                                           13, 8192, None)
+    assert st == 1 and b"k_tile" in lib.tmm_last_error(None)
+
+
+def test_library_exports_the_four_gemm_instantiations(tmm):
+    """gpu::gemm<S> is compiled into the library for the reference's four scalar types
+    (src/Tiled-MM/tiled_mm.cpp:626-668), so programs link against it as against the reference."""
+    out = subprocess.run(["nm", "-D", "--defined-only", "-C", str(tmm.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    for s in ("float", "double", "std::complex<float>", "std::complex<double>"):
+        assert f"void gpu::gemm<{s}" in out.replace("> >", ">>").replace("<float >", "<float>").replace(
+            "<double >", "<double>"), s
+
+
+def test_cmake_consumer_links_against_the_package(tmm, tmp_path):
+    """A downstream CMake project does find_package(Tiled-MM) and links Tiled-MM::Tiled-MM,
+    exactly as against the reference's package (CMakeLists.txt:42-63); it builds here (it runs on
+    a GPU only)."""
+    import shutil
+
+    if shutil.which("cmake") is None:
+        pytest.skip("cmake is not installed on this machine")
+    build = tmp_path / "build"
+    cfg = subprocess.run(["cmake", "-S", str(ROOT / "tests" / "cpp" / "consumer"), "-B", str(build),
+                          f"-DCMAKE_PREFIX_PATH={ROOT / 'tiled-mm_gb300' / 'tiledmm'}"], capture_output=True,
+                         text=True)
+    assert cfg.returncode == 0, cfg.stdout + cfg.stderr
+    bld = subprocess.run(["cmake", "--build", str(build)], capture_output=True, text=True)
+    assert bld.returncode == 0, bld.stdout + bld.stderr
+    exe = build / "consumer"
+    assert exe.exists()
+    needed = subprocess.run(["readelf", "-d", str(exe)], capture_output=True, text=True, check=True).stdout
+    assert "libtiledmm_gb300.so" in needed

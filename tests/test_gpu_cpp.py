@@ -32,3 +32,16 @@ def test_cpp_driver(driver, args):
     r = subprocess.run([str(driver), *args.split()], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "The result is CORRECT" in r.stdout
+
+
+def test_consumer_program_runs(tmm, tmp_path):
+    """The downstream program of tests/cpp/consumer (gpu::gemm from the library's explicit
+    instantiations for all four scalar types, the context's streams, events and device buffers),
+    built the way its CMake target would build it."""
+    exe = tmp_path / "consumer"
+    libdir = tmm.LIB_PATH.parent
+    subprocess.run(["g++", "-std=c++14", "-O2", "-DTILED_MM_CUDA", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cpp" / "consumer" / "main.cpp"), "-o", str(exe), "-L", str(libdir),
+                    "-ltiledmm_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "consumer OK" in r.stdout, r.stdout + r.stderr

@@ -264,6 +264,10 @@ def test_kernel_timing_counts_engine_launches(tmm):
     timed = run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
     sec, launches = ctx.kernel_time()
     assert launches == 8 and sec > 0
+    # launches of two compute streams may overlap: their union is at most their sum and at
+    # most the span from the first start to the last end
+    busy, span = ctx.kernel_busy_time()
+    assert 0 < busy <= sec * (1 + 1e-6) + 1e-6 and busy <= span * (1 + 1e-6) + 1e-6
     np.testing.assert_array_equal(timed, plain)
     ctx.set_kernel_timing(False)
     run(tmm, ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 0.5, c.copy(), ldc)
@@ -381,3 +385,59 @@ def test_autotune_tile_policy(tmm, ozaki):
     assert (tm, tn) == (m, n) and tk <= k  # everything fits: one C tile
     ctm, ctn, ctk = capped.get_tile_sizes()
     assert ctm * ctn * ctk < tm * tn * tk  # the cap forces smaller tiles
+
+
+def test_autotuner_times_candidates_then_keeps_the_fastest(tmm, tmp_path):
+    """TMM_TILE_POLICY_AUTOTUNE: the first calls of a size class each run one untimed candidate
+    (state 1), then every call uses the fastest measured one (state 2); every call computes the
+    whole product (integer inputs: exact under any tiling); the report names the candidates and
+    the choice, and a cache file carries the choice into a fresh process (state 3)."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    rng = np.random.default_rng(33)
+    m, n, k = 2500, 2300, 4100
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, kind="int09")
+    ref = tmm.make_context(np.float64, 2, 512, 512, 512)
+    exact = c.copy()
+    tmm.gemm(ref, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, exact, ldc)
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    ctx.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
+    seen, states = [], []
+    for _ in range(8):
+        cc = c.copy()
+        tmm.gemm(ctx, "N", "N", m, n, k, 1.0, a, lda, b, ldb, 1.0, cc, ldc)
+        np.testing.assert_array_equal(cc, exact)
+        st = ctx.stats()
+        states.append(st["autotune_state"])
+        seen.append((st["tile_m"], st["tile_n"], st["tile_k"]))
+        if st["autotune_state"] == 2:
+            break
+    assert states[-1] == 2 and set(states[:-1]) == {1}, states
+    explored = seen[:-1]
+    assert len(set(explored)) == len(explored) >= 2, explored  # distinct candidates, each timed once
+    assert seen[-1] in explored
+    report = ctx.autotune_report()
+    assert "(chosen)" in report and "TFLOP/s" in report, report
+    ctx.close()
+    ref.close()
+
+    cache = tmp_path / "tune.txt"
+    code = ("import sys, numpy as np; sys.path.insert(0, %r); import tiledmm as t;"
+            "ctx = t.make_context(np.float64, 2, 4096, 4096, 4096); ctx.set_tile_policy(t.TILE_POLICY_AUTOTUNE);"
+            "a = np.ones(%d); b = np.ones(%d); c = np.zeros(%d); states = []\n"
+            "for _ in range(8):\n"
+            "    t.gemm(ctx, 'N', 'N', %d, %d, %d, 1.0, a, %d, b, %d, 0.0, c, %d); s = ctx.stats(); states.append(s['autotune_state'])\n"
+            "    if s['autotune_state'] >= 2: break\n"
+            "assert c[0] == %d; print(states[-1], s['tile_m'], s['tile_n'], s['tile_k'])"
+            ) % (str(tmm.LIB_PATH.parents[1]), m * k, k * n, m * n, m, n, k, m, k, m, k)
+    env = dict(os.environ, TMM_AUTOTUNE_CACHE=str(cache))
+    first = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    assert first.returncode == 0, first.stderr
+    assert first.stdout.split()[0] == "2" and "tiles " in cache.read_text()
+    second = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    assert second.returncode == 0, second.stderr
+    assert second.stdout.split()[0] == "3"
+    assert second.stdout.split()[1:] == first.stdout.split()[1:]  # the cached choice is the measured one

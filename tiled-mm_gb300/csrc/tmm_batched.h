@@ -1,6 +1,8 @@
 // Internal interface of the batched persistent path and the autotuner (not part of the C ABI).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <string>
 #include <stdint.h>
 
 #include <vector>
@@ -42,9 +44,25 @@ int autotune_batch_variant(int dtype, int64_t m, int64_t n, int64_t k);
 struct TileChoice {
   int tm, tn, tk, streams;
 };
-// Tile sizes and stream count of the out-of-core pipeline for this problem and
-// device memory budget (TMM_TILE_POLICY_AUTOTUNE).
-TileChoice autotune_tiles(int dtype, bool ozaki, int slices, int64_t m, int64_t n, int64_t k, size_t budget_bytes,
-                          int max_tm, int max_tn, int max_tk);
+// What the tuner needs to know about a host-pointer call (TMM_TILE_POLICY_AUTOTUNE).
+struct TuneProblem {
+  int dtype, path, engine, slices;
+  int64_t m, n, k;
+  char ta, tb;
+  int pinned, copy_back;
+  size_t budget;  // device bytes the context may hold
+  int max_tm, max_tn, max_tk;
+};
+// The tile sizes and stream count for this call.  Measured tuning: each size class (dtype,
+// path, engine, slices, log2 buckets of m, n, k, trans, pinning, copy-back) has a few
+// candidates that fit the memory budget; the first calls of a class each run one untried
+// candidate (every call computes the full, correct product) and report their time through
+// autotune_report; once all are timed the fastest per flop is used, and it is appended to
+// the TMM_AUTOTUNE_CACHE file when one is named.  *index identifies the candidate for the
+// report (-1: the choice was read from the cache, nothing to report).
+TileChoice autotune_pick(const TuneProblem& p, int* index, int* state);
+void autotune_report(const TuneProblem& p, int index, double seconds);
+// Text of the measurements behind the tuner's choice for this problem's size class.
+std::string autotune_explain(const TuneProblem& p);
 
 }  // namespace tmm

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/tmm_c_api.h"
+#include "tmm_batched.h"
 
 namespace tmm {
 
@@ -119,7 +120,14 @@ struct tmm_context {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_pending, kt_free;
   double kt_seconds = 0.0;
   uint64_t kt_launches = 0;
+  // origin event recorded when timing is switched on; each timed launch's (start, end)
+  // relative to it, for the union of busy time over launches on several streams
+  cudaEvent_t kt_origin = nullptr;
+  std::vector<std::pair<double, double>> kt_intervals;
 
   tmm_stats stats{};
   std::string last_error;
+  // the size class of the last autotuned call (tmm_get_autotune_report)
+  tmm::TuneProblem last_tune{};
+  bool has_tune = false;
 };

@@ -342,6 +342,7 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
       cudaEventDestroy(ev.first);
       cudaEventDestroy(ev.second);
     }
+  if (ctx->kt_origin) cudaEventDestroy(ctx->kt_origin);
   ctx->batch_arena.release();
   ctx->batch_meta.release();
   ctx->batch_oz_scratch.release();
@@ -488,24 +489,61 @@ extern "C" int tmm_set_kernel_timing(tmm_context* ctx, int on) {
   ctx->kt_pending.clear();
   ctx->kt_seconds = 0.0;
   ctx->kt_launches = 0;
+  ctx->kt_intervals.clear();
   ctx->ktime = on != 0;
+  if (ctx->ktime) {
+    // the origin is recorded on the context's first stream before any timed launch
+    if (!ctx->kt_origin) TMM_CUDA(ctx, cudaEventCreate(&ctx->kt_origin));
+    TMM_CUDA(ctx, cudaEventRecord(ctx->kt_origin, ctx->streams.empty() ? (cudaStream_t)0 : ctx->streams[0]));
+  }
+  return TMM_SUCCESS;
+}
+
+// waits for the recorded launches and folds them into the totals and the interval list
+static int drain_kernel_timing(tmm_context* ctx) {
+  for (auto& ev : ctx->kt_pending) {
+    TMM_CUDA(ctx, cudaEventSynchronize(ev.second));
+    float ms = 0.0f, t0 = 0.0f, t1 = 0.0f;
+    TMM_CUDA(ctx, cudaEventElapsedTime(&ms, ev.first, ev.second));
+    ctx->kt_seconds += 1e-3 * (double)ms;
+    ctx->kt_launches++;
+    if (ctx->kt_origin && cudaEventElapsedTime(&t0, ctx->kt_origin, ev.first) == cudaSuccess &&
+        cudaEventElapsedTime(&t1, ctx->kt_origin, ev.second) == cudaSuccess)
+      ctx->kt_intervals.emplace_back(1e-3 * (double)t0, 1e-3 * (double)t1);
+    ctx->kt_free.push_back(ev);
+  }
+  ctx->kt_pending.clear();
   return TMM_SUCCESS;
 }
 
 extern "C" int tmm_get_kernel_time(tmm_context* ctx, double* seconds, uint64_t* launches) {
   if (!ctx || !seconds) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_kernel_time: null argument");
   DeviceGuard dg(ctx->device);
-  for (auto& ev : ctx->kt_pending) {
-    TMM_CUDA(ctx, cudaEventSynchronize(ev.second));
-    float ms = 0.0f;
-    TMM_CUDA(ctx, cudaEventElapsedTime(&ms, ev.first, ev.second));
-    ctx->kt_seconds += 1e-3 * (double)ms;
-    ctx->kt_launches++;
-    ctx->kt_free.push_back(ev);
-  }
-  ctx->kt_pending.clear();
+  if (int st = drain_kernel_timing(ctx)) return st;
   *seconds = ctx->kt_seconds;
   if (launches) *launches = ctx->kt_launches;
+  return TMM_SUCCESS;
+}
+
+extern "C" int tmm_get_kernel_busy_time(tmm_context* ctx, double* busy_seconds, double* span_seconds) {
+  if (!ctx || !busy_seconds) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_kernel_busy_time: null argument");
+  DeviceGuard dg(ctx->device);
+  if (int st = drain_kernel_timing(ctx)) return st;
+  std::vector<std::pair<double, double>> iv = ctx->kt_intervals;
+  std::sort(iv.begin(), iv.end());
+  double busy = 0.0, cur0 = 0.0, cur1 = -1.0;
+  for (const auto& x : iv) {
+    if (x.first > cur1) {  // a gap: close the current run of overlapping launches
+      if (cur1 > cur0) busy += cur1 - cur0;
+      cur0 = x.first;
+      cur1 = x.second;
+    } else if (x.second > cur1) {
+      cur1 = x.second;
+    }
+  }
+  if (cur1 > cur0) busy += cur1 - cur0;
+  *busy_seconds = busy;
+  if (span_seconds) *span_seconds = iv.empty() ? 0.0 : cur1 - iv.front().first;
   return TMM_SUCCESS;
 }
 
@@ -1008,6 +1046,8 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
 
   // ---- tile sizes (src/Tiled-MM/tiled_mm.cpp:557-560)
   int tm, tn, tk;
+  tmm::TuneProblem tune{};
+  int tune_index = -1;
   if (ctx->tile_policy == TMM_TILE_POLICY_REFERENCE) {
     tm = optimal_tile_size(m, ctx->cur_tile_m, ctx->max_tile_m);
     tn = optimal_tile_size(n, ctx->cur_tile_n, ctx->max_tile_n);
@@ -1017,9 +1057,25 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
     if (cudaMemGetInfo(&freeb, &total) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "cudaMemGetInfo");
     size_t budget = freeb + ctx->pool_a.capacity + ctx->pool_b.capacity + ctx->pool_c.capacity + ctx->staging.capacity;
     if (ctx->memory_limit) budget = std::min(budget, ctx->memory_limit);
-    const tmm::TileChoice tc = tmm::autotune_tiles(ctx->dtype, ctx->path == TMM_PATH_OZAKI, ctx->ozaki_slices > 0
-                                                   ? ctx->ozaki_slices : tmm::oz_default_slices(ctx->dtype), m, n, std::max<int64_t>(k, 1), budget,
-                                                   ctx->max_tile_m, ctx->max_tile_n, ctx->max_tile_k);
+    tune.dtype = ctx->dtype;
+    tune.path = ctx->path;
+    tune.engine = ctx->path == TMM_PATH_OZAKI ? ctx->oz_engine : 0;
+    tune.slices = ctx->path == TMM_PATH_OZAKI ? (ctx->ozaki_slices > 0 ? ctx->ozaki_slices
+                                                                      : tmm::oz_default_slices(ctx->dtype)) : 0;
+    tune.m = m;
+    tune.n = n;
+    tune.k = k;
+    tune.ta = trans_a;
+    tune.tb = trans_b;
+    tune.pinned = pin_host_buffers ? 1 : 0;
+    tune.copy_back = copy_c_back ? 1 : 0;
+    tune.budget = budget;
+    tune.max_tm = ctx->max_tile_m;
+    tune.max_tn = ctx->max_tile_n;
+    tune.max_tk = ctx->max_tile_k;
+    const tmm::TileChoice tc = tmm::autotune_pick(tune, &tune_index, &ctx->stats.autotune_state);
+    ctx->last_tune = tune;
+    ctx->has_tune = true;
     tm = tc.tm;
     tn = tc.tn;
     tk = tc.tk;
@@ -1078,7 +1134,18 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   unpin(pb);
   unpin(pc);
   ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!st && tune_index >= 0) tmm::autotune_report(tune, tune_index, ctx->stats.seconds);
   return st;
+}
+
+extern "C" int tmm_get_autotune_report(tmm_context* ctx, char* text, size_t capacity) {
+  if (!ctx || !text || capacity == 0) return fail(ctx, TMM_ERROR_INVALID_ARGUMENT, "tmm_get_autotune_report: bad argument");
+  const std::string r = ctx->has_tune ? tmm::autotune_explain(ctx->last_tune)
+                                      : std::string("no call of this context used the autotuner");
+  const size_t len = std::min(r.size(), capacity - 1);
+  memcpy(text, r.data(), len);
+  text[len] = 0;
+  return TMM_SUCCESS;
 }
 
 extern "C" int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,

@@ -57,6 +57,7 @@ SIGNATURES = {
     "tmm_gemm_device": (_ci, [_p, C.c_char, C.c_char, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64, _p]),
     "tmm_ozaki_gemm_device_noalloc": (_ci, [C.c_char, C.c_char, _i64, _i64, _i64, C.c_double, _p, _i64, _p, _i64,
                                             C.c_double, _p, _i64, _ci, _i64, _p]),
+    "tmm_ozaki_noalloc_status": (_ci, [_p]),
     "tmm_gemm_batched": (_ci, [_p, _ci, _p, _ci]),
     "tmm_xt_create": (_ci, [C.POINTER(_p)]),
     "tmm_xt_destroy": (_ci, [_p]),
@@ -69,6 +70,17 @@ SIGNATURES = {
     "tmm_xt_cgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
     "tmm_xt_zgemm": (_ci, [_p, _ci, _ci, _i64, _i64, _i64, _p, _p, _i64, _p, _i64, _p, _p, _i64]),
     "tmm_get_full_c": (_ci, [_p, C.POINTER(_p), C.POINTER(_sz), C.POINTER(_sz)]),
+    "tmm_get_stream": (_ci, [_p, _ci, C.POINTER(_p)]),
+    "tmm_get_result_stream": (_ci, [_p, C.POINTER(_p)]),
+    "tmm_get_device_buffer": (_ci, [_p, C.c_char, _ci, C.POINTER(_p)]),
+    "tmm_stream_create": (_ci, [C.POINTER(_p)]),
+    "tmm_stream_destroy": (_ci, [_p]),
+    "tmm_event_create": (_ci, [C.POINTER(_p)]),
+    "tmm_event_destroy": (_ci, [_p]),
+    "tmm_event_record": (_ci, [_p, _p]),
+    "tmm_event_synchronize": (_ci, [_p]),
+    "tmm_event_elapsed": (_ci, [_p, _p, C.POINTER(C.c_double)]),
+    "tmm_stream_wait_event": (_ci, [_p, _p]),
     "tmm_set_num_streams": (_ci, [_p, _ci]),
     "tmm_get_num_streams": (_ci, [_p, C.POINTER(_ci)]),
     "tmm_set_tile_sizes": (_ci, [_p, _ci, _ci, _ci]),
@@ -82,10 +94,12 @@ SIGNATURES = {
     "tmm_set_ozaki_engine": (_ci, [_p, _ci]),
     "tmm_get_ozaki_engine": (_ci, [_p, C.POINTER(_ci), C.POINTER(_ci), C.POINTER(_i64)]),
     "tmm_set_tile_policy": (_ci, [_p, _ci]),
+    "tmm_get_autotune_report": (_ci, [_p, C.c_char_p, _sz]),
     "tmm_set_memory_limit": (_ci, [_p, _sz]),
     "tmm_get_stats": (_ci, [_p, _p]),
     "tmm_set_kernel_timing": (_ci, [_p, _ci]),
     "tmm_get_kernel_time": (_ci, [_p, _p, _p]),
+    "tmm_get_kernel_busy_time": (_ci, [_p, _p, _p]),
     "tmm_last_error": (C.c_char_p, [_p]),
     "tmm_status_string": (C.c_char_p, [_ci]),
     "tmm_malloc_pinned": (_ci, [_sz, C.POINTER(_p)]),
@@ -112,7 +126,7 @@ class Stats(C.Structure):
     _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernels", C.c_uint64),
                 ("tiles_loaded", C.c_uint64), ("tiles_reused", C.c_uint64), ("tile_m", _ci), ("tile_n", _ci),
                 ("tile_k", _ci), ("n_streams", _ci), ("path", _ci), ("ozaki_slices", _ci), ("seconds", C.c_double),
-                ("batch_graph", _ci), ("direct_host", _ci), ("direct_bytes", C.c_uint64)]
+                ("batch_graph", _ci), ("direct_host", _ci), ("direct_bytes", C.c_uint64), ("autotune_state", _ci)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -262,6 +276,12 @@ class MMHandle:
     def set_tile_policy(self, policy: int) -> None:
         _check(_lib.tmm_set_tile_policy(self._h, policy), self._h)
 
+    def autotune_report(self) -> str:
+        """The autotuner's measured candidates and choice for this context's last autotuned call."""
+        buf = C.create_string_buffer(4096)
+        _check(_lib.tmm_get_autotune_report(self._h, buf, len(buf)), self._h)
+        return buf.value.decode()
+
     def set_memory_limit(self, nbytes: int) -> None:
         _check(_lib.tmm_set_memory_limit(self._h, nbytes), self._h)
 
@@ -274,6 +294,14 @@ class MMHandle:
         sec, n = C.c_double(), C.c_uint64()
         _check(_lib.tmm_get_kernel_time(self._h, C.byref(sec), C.byref(n)), self._h)
         return sec.value, n.value
+
+    def kernel_busy_time(self) -> tuple[float, float]:
+        """(busy seconds, span seconds) of the same launches: the union of their device
+        intervals (overlapping launches on several streams count once) and first start to
+        last end."""
+        busy, span = C.c_double(), C.c_double()
+        _check(_lib.tmm_get_kernel_busy_time(self._h, C.byref(busy), C.byref(span)), self._h)
+        return busy.value, span.value
 
     def stats(self) -> dict:
         s = Stats()
