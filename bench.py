@@ -87,11 +87,12 @@ WORKLOADS = {
     "cgemm8192": dict(m=8192, n=8192, k=8192, ta="N", tb="C", alpha=1.0, beta=0.0, kind=0, param=0.0,
                       path="embedded", dtype="complex64", tiles=(8192, 8192, 8192), streams=2,
                       desc="complex float GEMM m=n=k=8192, op(B) conjugate-transposed, uniform[-1,1) parts, "
-                           "device-resident: Ozaki path (real FP64 embedding, 6 slices) vs the native kernel"),
+                           "device-resident: the FP32 tensor-core engine (real embedding) vs the Ozaki path (FP64 "
+                           "embedding, 6 slices) and the FFMA kernel"),
     "sgemm16384": dict(m=16384, n=16384, k=16384, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
                        path="embedded", dtype="float32", tiles=(16384, 16384, 16384), streams=2,
-                       desc="float GEMM m=n=k=16384 NN, uniform[-1,1), device-resident: Ozaki path (FP64 "
-                            "embedding, 6 slices) vs the native FP32 kernel"),
+                       desc="float GEMM m=n=k=16384 NN, uniform[-1,1), device-resident: the FP32 tensor-core "
+                            "engine vs the Ozaki path (FP64 embedding, 6 slices) and the FFMA kernel"),
     "batched512": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=0.0, kind=0, param=0.0,
                        path="batched", tiles=(4096, 4096, 4096), streams=2,
                        desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
@@ -887,8 +888,14 @@ def run_embedded(args, w, rank, world, dist, log) -> dict:
     exact = A @ Bs.to(wide)
     den = A.abs() @ Bs.to(wide).abs()
     out = {}
-    for name in ("ozaki", "native"):
+    names = ("ozaki", "native") if npdt.type == np.complex128 else ("native", "ozaki", "native_simt")
+    for name in names:
+        # float and complex float: the native path is the FP32 tensor-core engine; the FFMA tile
+        # kernel it replaced (TMM_F32_KERNEL=simt) is timed beside it
+        if name == "native_simt":
+            os.environ["TMM_F32_KERNEL"] = "simt"
         ctx = tmm.make_context(npdt.type, w["streams"], *w["tiles"])
+        os.environ.pop("TMM_F32_KERNEL", None)
         if name == "ozaki":
             ctx.set_path(tmm.PATH_OZAKI, slices)
             ctx.set_ozaki_engine(w["engine"])
@@ -896,10 +903,11 @@ def run_embedded(args, w, rank, world, dist, log) -> dict:
         stream = torch.cuda.current_stream()
         call = lambda: tmm.gemm_device(ctx, w["ta"], w["tb"], m, n, k, 1.0, a, m, b, ldb, 0.0, c, m,
                                        stream=stream.cuda_stream)
-        for _ in range(args.warmup if name == "ozaki" else 1):
+        timed_path = "ozaki" if npdt.type == np.complex128 else "native"
+        for _ in range(args.warmup if name == timed_path else 1):
             call()
         torch.cuda.synchronize()
-        reps = args.steps if name == "ozaki" else 1
+        reps = args.steps if name == timed_path else 1
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(reps):
@@ -912,7 +920,8 @@ def run_embedded(args, w, rank, world, dist, log) -> dict:
         out[name] = {"tflops": flops / t / 1e12, "ms": t * 1e3, "max_componentwise_error": err}
         ctx.close()
     out["slices"] = slices
-    return {"value": out["ozaki"]["tflops"], "ms_per_step": out["ozaki"]["ms"], "embedded": out,
+    head = "ozaki" if npdt.type == np.complex128 else "native"
+    return {"value": out[head]["tflops"], "ms_per_step": out[head]["ms"], "path_timed": head, "embedded": out,
             "e2e": None, "gpu_launches": None}
 
 
@@ -984,8 +993,8 @@ def main() -> None:
         if rank == 0:
             line = dict(base)
             kind = {"complex128": "complex FP64", "complex64": "complex FP32", "float32": "FP32"}[w["dtype"]]
-            line["metric"] = (f"{kind} TFLOP/s ({'8' if 'complex' in w['dtype'] else '2'}mnk / time), Ozaki path vs "
-                              "the native kernel of the type")
+            line["metric"] = (f"{kind} TFLOP/s ({'8' if 'complex' in w['dtype'] else '2'}mnk / time) of the default "
+                              "path, beside the other paths of the type")
             line["dtype"] = {"complex128": "c128", "complex64": "c64", "float32": "f32"}[w["dtype"]]
             line.update(res)
             print(json.dumps(line), flush=True)

@@ -28,6 +28,8 @@
  *     pass_blocks k-blocks of kb elements (a pass never spans two groups);
  *     after each pass:  acc = acc + 2^(-w g) * S_pass   (one FP64 rounding).
  *  4. epilogue: t = acc * 2^(e_i + f_j - 2(w-1));
+ *     (a line holding an Inf or a NaN gets exponent 1025 and no digits; the product's
+ *     entries in its row or column are NaN)
  *     C = fma(alpha, t, beta * C)   (k-tile 0, C not read when beta == 0)
  *     C = fma(alpha, t, C)          (later k-tiles: beta' = 1)
  */
@@ -67,13 +69,17 @@ void tmmo_ozaki_split(const double* x, i64 ld, char op, i64 rows, i64 kk, i64 kp
   memset(digits, 0, (size_t)s * (size_t)rows * (size_t)kpad);
   for (i64 r = 0; r < rows; ++r) {
     double amax = 0;
+    int nonfinite = 0;
     for (i64 l = 0; l < kk; ++l) {
       double v = fabs(at(x, ld, o, r, l));
-      if (v > amax) amax = v;
+      if (!isfinite(v)) nonfinite = 1;
+      else if (v > amax) amax = v;
     }
-    int e = line_exponent(amax);
+    /* a line holding an Inf or a NaN: exponent 1025 (above every finite line exponent), no
+     * digits; its row or column of the product is NaN */
+    int e = nonfinite ? 1025 : line_exponent(amax);
     exps[r] = e;
-    if (amax == 0.0) continue;
+    if (amax == 0.0 || nonfinite) continue;
     for (i64 l = 0; l < kk; ++l) {
       double t = ldexp(at(x, ld, o, r, l), -e) * D;
       for (int p = 0; p < s; ++p) {
@@ -131,7 +137,9 @@ void tmmo_ozaki_gemm_split(i64 m, i64 n, i64 kpad, int s, int w, const int8_t* a
       }
       double t = ldexp(acc, ea[i] + eb[j] - 2 * (w - 1));
       double* cp = c + i + j * ldc;
-      if (!first_k_tile)
+      if (ea[i] >= 1025 || eb[j] >= 1025)
+        *cp = NAN;
+      else if (!first_k_tile)
         *cp = fma(alpha, t, *cp);
       else if (beta != 0.0)
         *cp = fma(alpha, t, beta * *cp);

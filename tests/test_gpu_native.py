@@ -5,7 +5,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from gpu_helpers import dense, exact_product, make_problem, tol_for
+from gpu_helpers import dense, exact_product, make_problem, op, tol_for
 from oracle_lib import oracle_gemm, reference_tiles
 
 pytestmark = pytest.mark.gpu
@@ -432,7 +432,7 @@ def test_autotuner_times_candidates_then_keeps_the_fastest(tmm, tmp_path):
             "    t.gemm(ctx, 'N', 'N', %d, %d, %d, 1.0, a, %d, b, %d, 0.0, c, %d); s = ctx.stats(); states.append(s['autotune_state'])\n"
             "    if s['autotune_state'] >= 2: break\n"
             "assert c[0] == %d; print(states[-1], s['tile_m'], s['tile_n'], s['tile_k'])"
-            ) % (str(tmm.LIB_PATH.parents[1]), m * k, k * n, m * n, m, n, k, m, k, m, k)
+            ) % (str(tmm.LIB_PATH.parents[2]), m * k, k * n, m * n, m, n, k, m, k, m, k)
     env = dict(os.environ, TMM_AUTOTUNE_CACHE=str(cache))
     first = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
     assert first.returncode == 0, first.stderr
@@ -441,3 +441,55 @@ def test_autotuner_times_candidates_then_keeps_the_fastest(tmm, tmp_path):
     assert second.returncode == 0, second.stderr
     assert second.stdout.split()[0] == "3"
     assert second.stdout.split()[1:] == first.stdout.split()[1:]  # the cached choice is the measured one
+
+
+@pytest.mark.parametrize("trans", ["NN", "NT", "TN", "TT"])
+@pytest.mark.parametrize("shape", [(300, 517, 1000), (129, 77, 4099), (1024, 768, 2048)])
+def test_fp32_tensor_core_engine_accuracy(tmm, monkeypatch, trans, shape):
+    """Float contexts multiply tiles on the tcgen05 tensor cores (three bf16 parts per FP32
+    value, six exact part products, FP32 accumulation): componentwise error against the FP64
+    product within 4 k 2^-24 (|alpha| |op(A)||op(B)| + |beta| |C|), and no worse than twice the
+    FFMA tile kernel's (TMM_F32_KERNEL=simt) on the same inputs."""
+    m, n, k = shape
+    ta, tb = trans
+    rng = np.random.default_rng(m + n + k)
+    a, lda, b, ldb, c, ldc = make_problem(rng, ta, tb, m, n, k, dtype=np.float32, pad=3)
+    A = op(a, lda, ta, m, k).astype(np.float64)
+    B = op(b, ldb, tb, k, n).astype(np.float64)
+    C0 = c.reshape(n, ldc).T[:m].astype(np.float64)
+    alpha, beta = 1.5, -0.75
+    exact = alpha * (A @ B) + beta * C0
+    bound = 4 * k * 2.0 ** -24 * (abs(alpha) * (np.abs(A) @ np.abs(B)) + abs(beta) * np.abs(C0))
+    errs = {}
+    for kernel in ("tc", "simt"):
+        if kernel == "simt":
+            monkeypatch.setenv("TMM_F32_KERNEL", "simt")
+        else:
+            monkeypatch.delenv("TMM_F32_KERNEL", raising=False)
+        ctx = tmm.make_context(np.float32, 2, 512, 512, 4096)
+        out = c.copy()
+        tmm.gemm(ctx, ta, tb, m, n, k, np.float32(alpha), a, lda, b, ldb, np.float32(beta), out, ldc)
+        ctx.close()
+        O = out.reshape(n, ldc).T[:m].astype(np.float64)
+        assert (np.abs(O - exact) <= bound).all(), kernel
+        errs[kernel] = float((np.abs(O - exact) / bound).max())
+    assert errs["tc"] <= 2 * errs["simt"] + 1e-3, errs
+
+
+def test_fp32_tensor_core_engine_nonfinite(tmm):
+    """An Inf or a NaN in the FP32 engine's operands reaches the product: the rows of op(A) and
+    columns of op(B) that hold one are not finite, every other entry is."""
+    rng = np.random.default_rng(3)
+    m, n, k = 200, 160, 300
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "N", m, n, k, dtype=np.float32)
+    a[4 + 9 * lda] = np.inf
+    b[20 + 7 * ldb] = np.nan  # column 7 of B
+    ctx = tmm.make_context(np.float32, 2, 4096, 4096, 4096)
+    out = c.copy()
+    tmm.gemm(ctx, "N", "N", m, n, k, np.float32(1.0), a, lda, b, ldb, np.float32(0.0), out, ldc)
+    O = out.reshape(n, ldc).T[:m]
+    mask = np.zeros((m, n), bool)
+    mask[4, :] = True
+    mask[:, 7] = True
+    assert not np.isfinite(O[mask]).any()
+    assert np.isfinite(O[~mask]).all()

@@ -360,3 +360,42 @@ def test_ozaki_default_slices_per_type(tmm):
         ctx.set_path(tmm.PATH_OZAKI, 99)
 
 
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("device", [False, True])
+def test_nonfinite_lines_give_nan(tmm, oracle, engine, device):
+    """An Inf or a NaN in a row of op(A) or a column of op(B) makes that row or column of the
+    product NaN (the digit split cannot represent it); every other entry keeps the oracle's bits.
+    Two k tiles: a non-finite value in the second k tile only still reaches its row."""
+    rng = np.random.default_rng(77)
+    m, n, k = 200, 150, 300
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k, kind="uexp")
+    a[3 + 10 * lda] = np.inf
+    a[17 + 250 * lda] = np.nan  # second k tile (tile_k 256)
+    b[5 + 7 * ldb] = -np.inf  # op(B) = B^T: column 5 of op(B) is row 5 of the stored B
+    ctx = ozaki_ctx(tmm, 7, (4096, 4096, 256), engine=engine)
+    eng = ctx.ozaki_engine()
+    if device:
+        torch = pytest.importorskip("torch")
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        dc = torch.from_numpy(c.copy()).cuda()
+        tmm.gemm_device(ctx, "N", "T", m, n, k, 1.5, da, lda, db, ldb, 0.5, dc, ldc,
+                        stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        out = dc.cpu().numpy()
+        tk = 256
+    else:
+        out = c.copy()
+        tmm.gemm(ctx, "N", "T", m, n, k, 1.5, a, lda, b, ldb, 0.5, out, ldc)
+        tk = reference_tiles(oracle, m, n, k, (4096, 4096, 256))[2]
+    want = ozaki_oracle(oracle, "N", "T", m, n, k, 1.5, a, lda, b, ldb, 0.5, c.copy(), ldc, 7, tk, eng["k_block"],
+                        eng["pass_blocks"])
+    O = out.reshape(n, ldc).T[:m]
+    W = want.reshape(n, ldc).T[:m]
+    nan_mask = np.zeros((m, n), bool)
+    nan_mask[[3, 17], :] = True
+    nan_mask[:, 5] = True
+    assert np.isnan(O[nan_mask]).all() and np.isnan(W[nan_mask]).all()
+    assert np.isfinite(O[~nan_mask]).all()
+    np.testing.assert_array_equal(O[~nan_mask], W[~nan_mask])

@@ -244,3 +244,26 @@ def test_float_default_slices_beat_fp32_accumulation(oracle, dist):
     e_fp32, e6 = err(acc.astype(np.float64)), err(oz(6))
     assert e6 < e_fp32 / 4
     assert e6 <= 2 * 2.0 ** -24  # within about one FP32 rounding of the result
+
+
+def test_ozaki_oracle_nonfinite_lines(oracle):
+    """The Ozaki restatement: a row of op(A) or a column of op(B) holding an Inf or a NaN gives a
+    NaN row or column of the product, and leaves every other entry as it is without them."""
+    from oracle_lib import ozaki_oracle
+
+    rng = np.random.default_rng(5)
+    m, n, k = 40, 30, 50
+    a = rng.uniform(-1, 1, m * k)
+    b = rng.uniform(-1, 1, k * n)
+    c = rng.uniform(-1, 1, m * n)
+    clean = ozaki_oracle(oracle, "N", "N", m, n, k, 1.0, a, m, b, k, 1.0, c.copy(), m, 6, k, 128, 512)
+    a2, b2 = a.copy(), b.copy()
+    a2[7 + 3 * m] = np.inf
+    b2[11 + 4 * k] = np.nan  # column 4 of B
+    out = ozaki_oracle(oracle, "N", "N", m, n, k, 1.0, a2, m, b2, k, 1.0, c.copy(), m, 6, k, 128, 512)
+    O, W = out.reshape(n, m).T, clean.reshape(n, m).T
+    assert np.isnan(O[7, :]).all() and np.isnan(O[:, 4]).all()
+    mask = np.ones((m, n), bool)
+    mask[7, :] = False
+    mask[:, 4] = False
+    np.testing.assert_array_equal(O[mask], W[mask])

@@ -24,7 +24,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", str(PKG.parent / "include"), "-I", str(CSRC)]
 
 SOURCES = ["tmm_core.cpp", "tmm_native.cu", "tmm_ozaki.cu", "tmm_tcgen05.cu", "tmm_batched.cu", "tmm_autotune.cpp",
-           "tmm_noalloc.cu", "tmm_xt.cpp", "tmm_ozaki_embed.cu", "tmm_dropin.cpp"]
+           "tmm_noalloc.cu", "tmm_xt.cpp", "tmm_ozaki_embed.cu", "tmm_dropin.cpp",
+           "tmm_f32tc.cu"]
 LIB = OUT / "libtiledmm_gb300.so"
 
 

@@ -160,7 +160,13 @@ std::vector<TileChoice> tile_candidates(const TuneProblem& p) {
     // two A tiles, two B tiles (cached form), four C tiles (2 streams x 2 slots), staging
     const double tile_a = ozaki ? (double)slices * a * c : (double)es * a * c;
     const double tile_b = ozaki ? (double)slices * b * c : (double)es * b * c;
-    return 2 * tile_a + 2 * tile_b + 4.0 * es * a * b + (ozaki ? 3.0 * 8 * std::max(a, b) * c : 0.0);
+    // float and complex float tiles on the FP32 tensor-core engine: per stream the bf16 parts
+    // (6 bytes per element of the embedded operands) and, for complex, the embedding and product
+    double f32 = 0.0;
+    if (!ozaki && dtype == TMM_FLOAT) f32 = 2.0 * 6.0 * (double)(a + b) * c;
+    if (!ozaki && dtype == TMM_COMPLEX_FLOAT)
+      f32 = 2.0 * (6.0 * (2.0 * a + b) * 2.0 * c + 4.0 * (4.0 * a * c + 2.0 * c * b + 2.0 * a * b));
+    return 2 * tile_a + 2 * tile_b + 4.0 * es * a * b + (ozaki ? 3.0 * 8 * std::max(a, b) * c : 0.0) + f32;
   };
   auto fit = [&](int64_t tm, int64_t tn, int64_t tk) {
     tm = std::max<int64_t>(1, std::min(tm, m));

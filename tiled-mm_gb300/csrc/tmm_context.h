@@ -127,6 +127,11 @@ struct tmm_context {
 
   tmm_stats stats{};
   std::string last_error;
+  // FP32 tensor-core engine: per stream slot (the compute streams, then one for other
+  // streams), a 256-byte error-word header and the bf16 planes of the tile operands
+  std::vector<tmm::GrowBuffer> f32_scratch;
+  bool f32_simt = false;  // TMM_F32_KERNEL=simt: the FFMA tile kernel instead
+
   // the size class of the last autotuned call (tmm_get_autotune_report)
   tmm::TuneProblem last_tune{};
   bool has_tune = false;

@@ -26,6 +26,7 @@
 #include <thread>
 
 #include "tmm_context.h"
+#include "tmm_f32tc.h"
 #include "tmm_kernels.h"
 #include "tmm_ozaki.h"
 #include "tmm_datagen.h"
@@ -137,10 +138,78 @@ struct KernelTimer {
   }
 };
 
+// Scratch of the FP32 tensor-core engine for launches on stream s (one buffer per compute
+// stream, one more for any other stream); its error word is zeroed when it is first allocated.
+int f32_scratch(tmm_context* ctx, cudaStream_t s, size_t bytes, void** ptr) {
+  size_t slot = ctx->streams.size();
+  for (size_t i = 0; i < ctx->streams.size(); ++i)
+    if (ctx->streams[i] == s) slot = i;
+  if (ctx->f32_scratch.size() <= slot) ctx->f32_scratch.resize(slot + 1);
+  tmm::GrowBuffer& buf = ctx->f32_scratch[slot];
+  const bool fresh = bytes > buf.capacity;
+  TMM_CUDA(ctx, buf.reserve(bytes));
+  if (fresh) TMM_CUDA(ctx, cudaMemset(buf.ptr, 0, 256));
+  *ptr = buf.ptr;
+  return TMM_SUCCESS;
+}
+
+// after synchronisation: a bounded wait of the FP32 engine that gave up
+int check_f32_error(tmm_context* ctx) {
+  for (auto& b : ctx->f32_scratch) {
+    if (!b.ptr) continue;
+    int word = 0;
+    TMM_CUDA(ctx, cudaMemcpy(&word, b.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (word) {
+      cudaMemset(b.ptr, 0, 256);
+      return fail(ctx, TMM_ERROR_TIMEOUT, "FP32 tensor-core kernel: a pipeline wait timed out");
+    }
+  }
+  return TMM_SUCCESS;
+}
+
 int launch_tile_gemm(tmm_context* ctx, Op opa, Op opb, int64_t m, int64_t n, int64_t k, const void* alpha,
                      const void* A, int64_t lda, const void* B, int64_t ldb, const void* beta, void* C,
                      int64_t ldc, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
+  if (ctx->dtype == TMM_COMPLEX_FLOAT && k > 0 && !ctx->f32_simt) {
+    // the per-tile cublasCgemm of src/Tiled-MM/tiled_mm.cpp:226-245: the real embedding
+    // [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B] (8mnk real flops, the complex count) on the
+    // FP32 tensor-core engine, then C = alpha (Re + i Im) + beta C
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t ahat = up((size_t)(2 * m) * (size_t)(2 * k) * 4), bhat = up((size_t)(2 * k) * (size_t)n * 4);
+    const size_t tbuf = up((size_t)(2 * m) * (size_t)n * 4);
+    const size_t eng = tmm::f32tc_scratch_bytes(2 * m, n, 2 * k);
+    void* scratch = nullptr;
+    if (int st = f32_scratch(ctx, s, eng + ahat + bhat + tbuf, &scratch)) return st;
+    TMM_CUDA(ctx, tmm::f32tc_prepare());
+    float* Ahat = (float*)((char*)scratch + eng);
+    float* Bhat = (float*)((char*)scratch + eng + ahat);
+    float* T = (float*)((char*)scratch + eng + ahat + bhat);
+    KernelTimer timer(ctx, s);
+    e = tmm::cplx_f32_embed(A, lda, opa, B, ldb, opb, m, n, k, Ahat, Bhat, s);
+    if (e == cudaSuccess)
+      e = tmm::f32tc_gemm(Op::OP_N, Op::OP_N, 2 * m, n, 2 * k, 1.0f, Ahat, 2 * m, Bhat, 2 * k, 0.0f, T, 2 * m, scratch,
+                          eng, s);
+    if (e == cudaSuccess) e = tmm::cplx_f32_combine(m, n, alpha, beta, T, C, ldc, s);
+    timer.done();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "complex FP32 tensor-core launch");
+    ctx->stats.kernels += 6;  // two embeddings, two splits, the product, the combine
+    return TMM_SUCCESS;
+  }
+  if (ctx->dtype == TMM_FLOAT && k > 0 && !ctx->f32_simt) {
+    // the per-tile cublasSgemm of src/Tiled-MM/tiled_mm.cpp:181-198 on the tcgen05 tensor cores
+    void* scratch = nullptr;
+    const size_t bytes = tmm::f32tc_scratch_bytes(m, n, k);
+    if (int st = f32_scratch(ctx, s, bytes, &scratch)) return st;
+    TMM_CUDA(ctx, tmm::f32tc_prepare());
+    KernelTimer timer(ctx, s);
+    e = tmm::f32tc_gemm(opa, opb, m, n, k, *(const float*)alpha, (const float*)A, lda, (const float*)B, ldb,
+                        *(const float*)beta, (float*)C, ldc, scratch, bytes, s);
+    timer.done();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "FP32 tensor-core launch");
+    ctx->stats.kernels += 3;  // two splits, the product
+    return TMM_SUCCESS;
+  }
   KernelTimer timer(ctx, s);
   switch (ctx->dtype) {
     case TMM_FLOAT:
@@ -283,6 +352,7 @@ extern "C" int tmm_create(int dtype, int n_streams, int max_tile_m, int max_tile
   ctx->max_tile_n = max_tile_n;
   ctx->max_tile_k = max_tile_k;
   ctx->oz_engine = tmm::ozaki_default_engine();
+  if (const char* f32 = getenv("TMM_F32_KERNEL")) ctx->f32_simt = strcmp(f32, "simt") == 0;
   cudaError_t e = cudaGetDevice(&ctx->device);
   if (e == cudaSuccess) {
     int pageable = 0, host_tables = 0;
@@ -347,6 +417,7 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   ctx->batch_meta.release();
   ctx->batch_oz_scratch.release();
   for (auto& b : ctx->cz_scratch) b.release();
+  for (auto& b : ctx->f32_scratch) b.release();
   for (auto b : ctx->oz_branches) cudaStreamDestroy(b);
   for (auto e : ctx->oz_branch_done) cudaEventDestroy(e);
   if (ctx->oz_fork) cudaEventDestroy(ctx->oz_fork);
@@ -1130,6 +1201,7 @@ extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m,
   int st2 = sync_all(ctx);  // returns with C final (the reference syncs the device: tiled_mm.cpp:602-604)
   if (!st) st = st2;
   if (!st && (ozaki || P.embed)) st = check_oz_error(ctx);
+  if (!st && (ctx->dtype == TMM_FLOAT || ctx->dtype == TMM_COMPLEX_FLOAT)) st = check_f32_error(ctx);
   unpin(pa);
   unpin(pb);
   unpin(pc);

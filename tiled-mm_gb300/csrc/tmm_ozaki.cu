@@ -368,7 +368,8 @@ oz_gemm_imma(const uint8_t* __restrict__ Ad, const int32_t* __restrict__ ea, int
         if (gi < m && gj < n) {
           double t = scalbn(facc[row * IM_BN + col], ea[gi] + eb[gj] - 2 * (OZ_DIGIT_BITS - 1));
           double* cp = C + gi + gj * ldc;
-          if (!first) *cp = fma(alpha, t, *cp);
+          if (ea[gi] >= OZ_EXP_NONFINITE || eb[gj] >= OZ_EXP_NONFINITE) *cp = __longlong_as_double(0x7FF8000000000000ll);
+          else if (!first) *cp = fma(alpha, t, *cp);
           else if (beta != 0.0) *cp = fma(alpha, t, beta * *cp);
           else *cp = alpha * t;
         }

@@ -19,6 +19,11 @@ constexpr int OZ_ROW_ALIGN = 256;  // lines are padded to the GEMM tiles (128 x 
 constexpr int OZ_K_ALIGN = 128;    // k is padded to whole k-blocks (bytes)
 constexpr int OZ_DIGIT_BITS = 5;   // |d| <= 2^(w-1) = 16: exact in int8 and in e4m3
 constexpr int OZ_MAX_SLICES = 20;
+// Line exponent of a line (row of op(A), column of op(B)) holding an Inf or a NaN: the frexp
+// exponent of the largest finite magnitude is at most 1024, and the line maximum taken over
+// the IEEE bits of |x| puts any non-finite value above every finite one.  The product's
+// entries in such a row or column are NaN (IEEE arithmetic would give +-Inf for some of them).
+constexpr int OZ_EXP_NONFINITE = 1025;
 constexpr int OZ_DEFAULT_SLICES = 13;
 // float and complex float contexts: 6 slices (30 bits per line) leave the product within a
 // few units of FP32 rounding, below the error of an FP32-accumulating GEMM

@@ -10,6 +10,7 @@
 // embedding.  A combine kernel applies alpha and beta and rounds once to the output type.
 #include <cuda_runtime.h>
 
+#include "tmm_f32tc.h"
 #include "tmm_ozaki.h"
 
 namespace tmm {
@@ -45,9 +46,9 @@ constexpr bool is_complex() {
 
 // Ahat of op(A) (m x k).  Transposed operands go through a shared-memory tile so that
 // both the reads of A and the writes of Ahat are coalesced.
-template <typename T>
+template <typename T, typename O = double>
 __global__ void embed_a_kernel(const T* __restrict__ A, int64_t lda, Op op, int64_t m, int64_t k,
-                               double* __restrict__ Ahat) {
+                               O* __restrict__ Ahat) {
   __shared__ double2 tile[TT][TT + 1];
   const int64_t i0 = (int64_t)blockIdx.x * TT, l0 = (int64_t)blockIdx.y * TT;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
@@ -65,19 +66,19 @@ __global__ void embed_a_kernel(const T* __restrict__ A, int64_t lda, Op op, int6
     const int64_t i = i0 + tx, l = l0 + r;
     if (i >= m || l >= k) continue;
     const double2 v = tile[r][tx];
-    Ahat[i + l * mm] = v.x;  // (top-left): Re A
+    Ahat[i + l * mm] = (O)v.x;  // (top-left): Re A
     if (is_complex<T>()) {
-      Ahat[(m + i) + l * mm] = v.y;        // bottom-left: Im A
-      Ahat[i + (k + l) * mm] = -v.y;       // top-right: -Im A
-      Ahat[(m + i) + (k + l) * mm] = v.x;  // bottom-right: Re A
+      Ahat[(m + i) + l * mm] = (O)v.y;        // bottom-left: Im A
+      Ahat[i + (k + l) * mm] = (O)-v.y;       // top-right: -Im A
+      Ahat[(m + i) + (k + l) * mm] = (O)v.x;  // bottom-right: Re A
     }
   }
 }
 
 // Bhat of op(B) (k x n): op(B) itself, or [Re; Im] for complex
-template <typename T>
+template <typename T, typename O = double>
 __global__ void embed_b_kernel(const T* __restrict__ B, int64_t ldb, Op op, int64_t k, int64_t n,
-                               double* __restrict__ Bhat) {
+                               O* __restrict__ Bhat) {
   __shared__ double2 tile[TT][TT + 1];
   const int64_t l0 = (int64_t)blockIdx.x * TT, j0 = (int64_t)blockIdx.y * TT;
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -95,8 +96,8 @@ __global__ void embed_b_kernel(const T* __restrict__ B, int64_t ldb, Op op, int6
     const int64_t l = l0 + tx, j = j0 + r;
     if (l >= k || j >= n) continue;
     const double2 v = tile[r][tx];
-    Bhat[l + j * kk] = v.x;
-    if (is_complex<T>()) Bhat[(k + l) + j * kk] = v.y;
+    Bhat[l + j * kk] = (O)v.x;
+    if (is_complex<T>()) Bhat[(k + l) + j * kk] = (O)v.y;
   }
 }
 
@@ -133,14 +134,14 @@ __device__ __forceinline__ void st_c<double2>(double2* p, double2 v) {
 // beta' == 0 on the first k tile: C is not read.  Real: fma(alpha, t, beta c) / alpha t /
 // fma(alpha, t, c), as the real engine's epilogue.  Complex: the products of alpha and
 // beta with a complex value each take one fma per component.
-template <typename T>
+template <typename T, typename TE = double>
 __global__ void combine_kernel(int64_t m, int64_t n, double2 alpha, double2 beta, int first,
-                               const double* __restrict__ Tm, T* __restrict__ C, int64_t ldc) {
+                               const TE* __restrict__ Tm, T* __restrict__ C, int64_t ldc) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (i >= m || j >= n) return;
   T* cp = C + i + j * ldc;
   if (!is_complex<T>()) {
-    const double t = Tm[i + j * m];
+    const double t = (double)Tm[i + j * m];
     double r;
     if (!first) r = fma(alpha.x, t, ld_c<T>(cp).x);
     else if (beta.x != 0.0) r = fma(alpha.x, t, beta.x * ld_c<T>(cp).x);
@@ -148,7 +149,7 @@ __global__ void combine_kernel(int64_t m, int64_t n, double2 alpha, double2 beta
     st_c<T>(cp, make_double2(r, 0.0));
     return;
   }
-  const double tr = Tm[i + j * 2 * m], ti = Tm[m + i + j * 2 * m];
+  const double tr = (double)Tm[i + j * 2 * m], ti = (double)Tm[m + i + j * 2 * m];
   double2 r;
   r.x = fma(alpha.x, tr, -alpha.y * ti);
   r.y = fma(alpha.x, ti, alpha.y * tr);
@@ -188,6 +189,34 @@ cudaError_t combine_t(int64_t m, int64_t n, double2 alpha, double2 beta, bool fi
 }
 
 }  // namespace
+
+// Complex float on the FP32 tensor-core engine: the same real embedding in float (exact), and
+// C = alpha * T + beta * C from the engine's float product T (2m x n: Re C over Im C),
+// computed in double and rounded once to complex float.
+cudaError_t cplx_f32_embed(const void* A, int64_t lda, Op opa, const void* B, int64_t ldb, Op opb, int64_t m,
+                           int64_t n, int64_t k, float* Ahat, float* Bhat, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return cudaSuccess;
+  if ((k + TT - 1) / TT > 65535 || (n + TT - 1) / TT > 65535) return cudaErrorInvalidValue;  // grid y
+  const dim3 block(TT, 8);
+  embed_a_kernel<float2, float><<<dim3((unsigned)((m + TT - 1) / TT), (unsigned)((k + TT - 1) / TT)), block, 0, s>>>(
+      (const float2*)A, lda, opa, m, k, Ahat);
+  embed_b_kernel<float2, float><<<dim3((unsigned)((k + TT - 1) / TT), (unsigned)((n + TT - 1) / TT)), block, 0, s>>>(
+      (const float2*)B, ldb, opb, k, n, Bhat);
+  return cudaGetLastError();
+}
+
+cudaError_t cplx_f32_combine(int64_t m, int64_t n, const void* alpha, const void* beta, const float* Tm, void* C,
+                             int64_t ldc, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return cudaSuccess;
+  const double2 al = make_double2((double)((const float*)alpha)[0], (double)((const float*)alpha)[1]);
+  const double2 be = make_double2((double)((const float*)beta)[0], (double)((const float*)beta)[1]);
+  for (int64_t j0 = 0; j0 < n; j0 += 65535) {  // grid y is 16-bit: column panels
+    const int64_t nn = n - j0 < 65535 ? n - j0 : 65535;
+    combine_kernel<float2, float><<<dim3((unsigned)((m + 255) / 256), (unsigned)nn), 256, 0, s>>>(
+        m, nn, al, be, 1, Tm + j0 * 2 * m, (float2*)C + j0 * ldc, ldc);
+  }
+  return cudaGetLastError();
+}
 
 bool ozaki_embedded_dtype(int dtype) {
   return dtype == TMM_FLOAT || dtype == TMM_COMPLEX_FLOAT || dtype == TMM_COMPLEX_DOUBLE;

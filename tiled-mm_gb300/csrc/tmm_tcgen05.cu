@@ -36,6 +36,7 @@
 #include <mutex>
 
 #include "tmm_ozaki.h"
+#include "tmm_tc_ptx.cuh"
 
 namespace tmm {
 namespace tc {
@@ -47,117 +48,11 @@ constexpr int THREADS = 192;
 constexpr int TMEM_COLS = 512;
 constexpr int64_t PASS_BLOCKS = 512;  // 512 * 128 = 65536 k terms per exact FP32 pass
 constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
-constexpr unsigned long long WAIT_NS = 1000000000ull;  // one second per wait
 constexpr size_t WORK_HEADER = 256;  // bytes before the accumulator slots: the pacing counter
 // the epilogue waits a whole pass (tens of microseconds) for an accumulator: park, don't spin
 constexpr uint32_t EPI_WAIT_HINT_NS = 20000;
 
-// ------------------------------------------------------------------ PTX wrappers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// try_wait that may park the thread up to hint_ns nanoseconds (it resumes when the phase
-// completes): for waits that are long and not latency-critical
-__device__ __forceinline__ bool mbar_try_wait_hint(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity), "r"(hint_ns)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false after WAIT_NS (error word set) or when another role gave up.
-// hint_ns > 0: park between probes (mbar_try_wait_hint) instead of spinning.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
-                                          uint32_t hint_ns = 0) {
-  if (!hint_ns)
-    for (int i = 0; i < 256; ++i)
-      if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
-  while (true) {
-    if (hint_ns ? mbar_try_wait_hint(bar, parity, hint_ns) : mbar_try_wait(bar, parity)) return true;
-    if (*abort_flag) return false;
-    if (globaltimer() - t0 > WAIT_NS) {
-      *abort_flag = 1;
-      atomicOr(err, 1);
-      return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// L2 prefetch of the box at (x, y): a hint, nothing waits for it
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
-  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)map), "r"(x), "r"(y)
-               : "memory");
-}
-
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t slot_smem, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_smem), "r"(ncols));
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
-}
-
-// K-major operand, 128-byte swizzle, 8-row core groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFF) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
-  d |= (uint64_t)1 << 46;                  // descriptor version (tcgen05)
-  d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
-  return d;
-}
-
+// ------------------------------------------------------------------ f8 MMA forms
 // kind::f8f6f4: D f32, A e4m3, B e4m3, both K-major, N = 256, M = 128
 constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
@@ -168,77 +63,6 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
       "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
 }
 
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-// ---- CTA-pair (cta_group::2) forms
-__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t cta) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(cta));
-  return r;
-}
-
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait of the pair engine.  A timeout raises this CTA's and the peer's
-// abort flags; with honor_abort false (the final drains) only the timeout ends it,
-// so copies and MMAs in flight finish before TMEM is freed.  CLUSTER_ACQ: acquire
-// at cluster scope (a barrier that the peer's threads arrive on); copies and MMA
-// commits signal their barriers through the async proxy and need only the default.
-template <bool CLUSTER_ACQ>
-__device__ __forceinline__ bool mbar_wait_pair(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                               uint32_t peer_abort, int* err, bool honor_abort = true,
-                                               uint32_t hint_ns = 0) {
-  auto probe = [&] {
-    if (CLUSTER_ACQ) return mbar_try_wait_cluster(bar, parity);
-    return hint_ns ? mbar_try_wait_hint(bar, parity, hint_ns) : mbar_try_wait(bar, parity);
-  };
-  for (int i = 0; i < 256; ++i)
-    if (probe()) return true;
-  const uint64_t t0 = globaltimer();
-  while (true) {
-    if (probe()) return true;
-    if (honor_abort && *abort_flag) return false;
-    if (globaltimer() - t0 > WAIT_NS) {
-      *abort_flag = 1;
-      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(peer_abort), "r"(1) : "memory");
-      atomicOr(err, 1);
-      return false;
-    }
-  }
-}
-
-// the leader's and the peer's TMEM allocation is one collective (one warp in each CTA)
-__device__ __forceinline__ void tmem_alloc_pair(uint32_t slot_smem, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_smem), "r"(ncols));
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
-}
-__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
-}
-
-// copy into this CTA's shared memory, bytes counted on the (leader's) barrier at a cluster address
-__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar_cluster) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar_cluster)
-      : "memory");
-}
-
 // kind::f8f6f4 across the pair: M = 256 (128 TMEM lanes in each CTA), N = 256
 constexpr uint32_t IDESC_PAIR = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
 
@@ -247,35 +71,6 @@ __device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uin
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(adesc), "l"(bdesc), "r"(IDESC_PAIR), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
-               "h"(mask)
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-// wait for this thread's tcgen05.ld; the loaded registers are operands so that no use of
-// them is scheduled before it
-__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.wait::ld.sync.aligned;"
-      : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]),
-        "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]),
-        "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]),
-        "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
-      :
-      : "memory");
 }
 
 // ------------------------------------------------------------------ work sequence
@@ -485,7 +280,8 @@ __device__ __forceinline__ void drain_pass(uint32_t tbase, double* __restrict__ 
         if (h + j >= nv) break;
         const double t = scalbn_fast(acc[h + j], ei + fj[j] - 2 * (OZ_DIGIT_BITS - 1));
         double out;
-        if (plain) out = t;
+        if (ei >= OZ_EXP_NONFINITE || fj[j] >= OZ_EXP_NONFINITE) out = __longlong_as_double(0x7FF8000000000000ll);
+        else if (plain) out = t;
         else if (!P.first) out = fma(P.alpha, t, cv[j]);
         else if (P.beta != 0.0) out = fma(P.alpha, t, P.beta * cv[j]);
         else out = P.alpha * t;
@@ -1080,8 +876,21 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   P.pace = (unsigned long long*)work;
   P.work = (double*)((char*)work + tc::WORK_HEADER);
   P.err = err;
-  P.pace_lag = 0;
-  P.pace_chunk = 16;
+  // Engine form: CTA pairs issuing cta_group::2 MMAs on 256 x 256 tiles from two 128-row
+  // tiles up (their operand traffic per SM is two thirds of the one-SM form's and a ring of
+  // six 32 KB stages looks ahead 1.5x as far), else one CTA per SM on 128 x 256 tiles;
+  // TMM_TC_CLUSTER=1 or =pair forces a form.  Wave pacing (lag 2 chunks of 64 k-blocks) is
+  // on for the pair form, which drifts apart without it, and off for the one-SM form, which
+  // it slowed by 2-4 %.  Measured at m = n = 32768, k = 16384, 11 slices, under the power
+  // limit: one-SM 740 ms, pair 875 ms, pair with pacing 694 ms per launch; at m = n = 8192:
+  // 46.5, 43.4, 43.3 ms.
+  int cm = (m + tc::BM - 1) / tc::BM >= 2 ? 0 : 1;  // 0: pair
+  if (const char* env = getenv("TMM_TC_CLUSTER")) {
+    if (!strcmp(env, "pair")) cm = 0;
+    else if (!strcmp(env, "1")) cm = 1;
+  }
+  P.pace_lag = cm == 0 ? 2 : 0;
+  P.pace_chunk = 64;
   P.pace_ns = 20000;
   if (const char* env = getenv("TMM_TC_PACE")) P.pace_lag = atoi(env) < 0 ? 0 : atoi(env);
   if (const char* env = getenv("TMM_TC_PACE_CHUNK")) {
@@ -1096,12 +905,6 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   if (const char* env = getenv("TMM_TC_EPI_HINT_NS")) P.epi_hint = (uint32_t)(atoi(env) < 0 ? 0 : atoi(env));
   P.pf = 0;  // measured: any distance (4..32) slows the 8192^3 and 8192^2 x 32768 runs by 30-120 %
   if (const char* env = getenv("TMM_TC_PREFETCH")) P.pf = atoi(env) < 0 ? 0 : (atoi(env) > 64 ? 64 : atoi(env));
-  // Engine form: one CTA per SM on 128 x 256 tiles (default), or with TMM_TC_CLUSTER=pair
-  // CTA pairs issuing cta_group::2 MMAs on 256 x 256 tiles.  Cycles per k-block and SM,
-  // 11 slices: 8192^3 -> 893 (one SM), 896 (pair); 16384^3 -> 925 (pair); 32768^3 -> 1134 (pair).
-  int cm = 1;  // 0: pair
-  if (const char* env = getenv("TMM_TC_CLUSTER"))
-    if (!strcmp(env, "pair")) cm = 0;
   if (cm == 0) {
     if (A.rows_pad % tc::PAIR_M) return cudaErrorInvalidValue;
     P.tiles_m = (int)((m + tc::PAIR_M - 1) / tc::PAIR_M);
