@@ -109,6 +109,9 @@ def test_device_operands(tmm, oracle):
 
 @pytest.mark.parametrize("tile", ["64", "128"])
 def test_fp32_tile_variants(tmm, oracle, monkeypatch, tile):
+    """The grouped FFMA kernel's two tile shapes (TMM_F32_KERNEL=simt; by default a batch's
+    FP32 problems run on the FP32 tensor-core engine)."""
+    monkeypatch.setenv("TMM_F32_KERNEL", "simt")
     monkeypatch.setenv("TMM_BATCH_F32_TILE", tile)
     rng = np.random.default_rng(4)
     probs = [p for p in make_batch(rng, 16, sizes=(100, 700), kmax=500) if p["a"].dtype == np.float32]
@@ -204,14 +207,12 @@ def check_ozaki(oracle, probs, c0s, slices, tk, eng, f32_on_engine=False, slices
 
 
 @pytest.mark.parametrize("engine", ["tcgen05", "imma"])
-@pytest.mark.parametrize("f32_on_engine", [False, True])
-def test_ozaki_batch_bit_exact(tmm, oracle, monkeypatch, engine, f32_on_engine):
+def test_ozaki_batch_bit_exact(tmm, oracle, engine):
     """On an Ozaki context the batch's FP64 problems (uneven shapes, N/T/C, k == 0, several k
-    tiles of max_tile_k) run on the engine and equal the oracle's Ozaki product bit for bit;
-    FP32 problems stay on the grouped kernel, or with TMM_BATCH_OZ_F32=1 run on the engine
-    through their FP64 embedding at the float default of 6 slices, also bit for bit."""
-    if f32_on_engine:
-        monkeypatch.setenv("TMM_BATCH_OZ_F32", "1")
+    tiles of max_tile_k) run on the engine -- the tcgen05 engine in one grouped launch per
+    chunk and k-tile round -- and equal the oracle's Ozaki product bit for bit; FP32 problems
+    stay on the grouped FP32 kernel."""
+    f32_on_engine = False
     rng = np.random.default_rng(11)
     probs = ozaki_batch(rng, 24, sizes=(1, 400), kmax=400)
     c0s = [p["c"].copy() for p in probs]
@@ -264,3 +265,26 @@ def test_ozaki_batch_graph_capture_replay_and_device_operands(tmm, oracle):
         np.testing.assert_array_equal(d["c"].cpu().numpy(), h)
     for pa in keep:
         pa.free()
+
+
+def test_fp32_problems_on_the_tensor_core_engine(tmm, oracle):
+    """A batch's FP32 problems (uneven shapes, N/T, k == 0 among them) run in one grouped launch
+    of the FP32 tensor-core engine, FP32-accurate against the oracle, from host and from device
+    operands, and the FP64 problems beside them on their own kernel."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    probs = make_batch(rng, 30, sizes=(1, 900), kmax=1500)
+    c0s = [p["c"].copy() for p in probs]
+    ctx = tmm.make_context(np.float64, 2, 4096, 4096, 4096)
+    tmm.gemm_batched(ctx, probs)
+    check(oracle, probs, c0s)
+    dev = []
+    for p, c0 in zip(probs, c0s):
+        d = dict(p)
+        d["a"], d["b"], d["c"] = (torch.from_numpy(x.copy()).cuda() for x in (p["a"], p["b"], c0))
+        d["dtype"] = p["a"].dtype
+        dev.append(d)
+    tmm.gemm_batched(ctx, dev, device_operands=True)
+    for p, d in zip(probs, dev):
+        p["c"][:] = d["c"].cpu().numpy()
+    check(oracle, probs, c0s)

@@ -130,6 +130,11 @@ struct tmm_context {
   // FP32 tensor-core engine: per stream slot (the compute streams, then one for other
   // streams), a 256-byte error-word header and the bf16 planes of the tile operands
   std::vector<tmm::GrowBuffer> f32_scratch;
+  // batched FP32 problems on that engine: [error word][planes][grouped launch records], and the
+  // stream they run on beside the batch stream
+  tmm::GrowBuffer batch_f32_scratch;
+  cudaStream_t batch_f32_stream = nullptr;
+  cudaEvent_t batch_f32_fork = nullptr, batch_f32_join = nullptr;
   bool f32_simt = false;  // TMM_F32_KERNEL=simt: the FFMA tile kernel instead
 
   // the size class of the last autotuned call (tmm_get_autotune_report)

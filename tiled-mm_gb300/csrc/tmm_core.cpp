@@ -15,6 +15,7 @@
 // are ordered against compute with events only; each compute stream owns two
 // C tile slots, so the copy-back of one tile overlaps the next tile's k loop.
 #include <algorithm>
+#include <numeric>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -155,7 +156,11 @@ int f32_scratch(tmm_context* ctx, cudaStream_t s, size_t bytes, void** ptr) {
 
 // after synchronisation: a bounded wait of the FP32 engine that gave up
 int check_f32_error(tmm_context* ctx) {
-  for (auto& b : ctx->f32_scratch) {
+  std::vector<tmm::GrowBuffer*> bufs;
+  for (auto& b : ctx->f32_scratch) bufs.push_back(&b);
+  bufs.push_back(&ctx->batch_f32_scratch);
+  for (tmm::GrowBuffer* bp : bufs) {
+    tmm::GrowBuffer& b = *bp;
     if (!b.ptr) continue;
     int word = 0;
     TMM_CUDA(ctx, cudaMemcpy(&word, b.ptr, sizeof(int), cudaMemcpyDeviceToHost));
@@ -416,6 +421,10 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   ctx->batch_arena.release();
   ctx->batch_meta.release();
   ctx->batch_oz_scratch.release();
+  ctx->batch_f32_scratch.release();
+  if (ctx->batch_f32_stream) cudaStreamDestroy(ctx->batch_f32_stream);
+  if (ctx->batch_f32_fork) cudaEventDestroy(ctx->batch_f32_fork);
+  if (ctx->batch_f32_join) cudaEventDestroy(ctx->batch_f32_join);
   for (auto& b : ctx->cz_scratch) b.release();
   for (auto& b : ctx->f32_scratch) b.release();
   for (auto b : ctx->oz_branches) cudaStreamDestroy(b);
@@ -1414,20 +1423,31 @@ void drop_batch_graph(tmm_context* ctx) {
   ctx->batch_key.clear();
 }
 
-// FP64 problems of a batch on the Ozaki path (context path TMM_PATH_OZAKI): per problem and
-// k tile of at most max_tile_k, the split of op(A) and op(B) and one engine launch, as
-// tmm_gemm_device does, so each result equals that call's bit for bit.  The problems run
-// concurrently on branch streams forked from and joined into the batch stream, spread
-// largest first over the least-loaded branch; a branch reuses one digit-plane scratch
-// region and one engine workspace (sized for its largest launch) for its problems in turn.
-constexpr int BATCH_OZ_BRANCHES = 256;  // measured on 256 FP64 problems: 64 -> 104 ms, 128 -> 98, 256 -> 78 per call
+// FP64 problems of a batch on the Ozaki path (context path TMM_PATH_OZAKI).  Each problem is
+// split per k tile of at most max_tile_k, as tmm_gemm_device does, so each result equals that
+// call's bit for bit; the split planes of all problems live in one arena, and the tcgen05 engine
+// multiplies every problem of a chunk in one persistent launch over their tiles
+// (ozaki_gemm_tc_grouped).  The problems are cut into chunks of about equal work; with host
+// operands, chunk c's copies in run on a copy stream, its splits and grouped launches on a
+// compute stream once they have landed, and its copies out on a third stream, so the host
+// link in both directions overlaps the products of the other chunks.  The three streams fork
+// from the batch stream and join it.  The IMMA engine runs the same pipeline with one launch
+// per problem and k tile.
+constexpr int BATCH_OZ_CHUNKS = 4;
 
+struct BatchOzRound {  // one grouped launch: the chunk's problems that have a k tile r
+  int chunk, round, n_probs, n_items;
+  size_t image_off;  // its device records in the batch scratch
+};
 struct BatchOzPlan {
-  std::vector<std::vector<int>> branch;  // problem indices per branch, in launch order
-  std::vector<size_t> offset;            // scratch offset of each branch: [engine workspace][problem scratch]
-  std::vector<size_t> work_bytes;        // engine workspace of each branch
-  int slices = 0;      // FP64 problems
-  int slices_f32 = 0;  // FP32 problems (the product of their FP64 embedding)
+  std::vector<int> ids;                 // FP64 problems on the engine
+  std::vector<int64_t> tk;              // per id: k tile
+  std::vector<size_t> a_off, b_off;     // per id: split planes in the arena
+  std::vector<int> chunk_of;            // per id
+  std::vector<std::vector<int>> chunks;  // positions in ids, per chunk
+  std::vector<BatchOzRound> launches;
+  int slices = 0;
+  size_t work_off = 0, arena_off = 0, arena_bytes = 0;
   int kernels = 0;
 };
 
@@ -1439,72 +1459,119 @@ int batch_slices(const tmm_context* ctx, int dtype) {
   return ctx->ozaki_slices > 0 && ctx_single == single ? ctx->ozaki_slices : tmm::oz_default_slices(dtype);
 }
 
-// device scratch of one batch problem on the Ozaki path, per k tile of tk: the digit planes
-// (FP64), or the FP64 embedding Ahat (m x tk), Bhat (tk x n), its product T (m x n) and their
-// digit planes (FP32)
-struct BatchOzScratch {
-  size_t ahat = 0, bhat = 0, t = 0, sa = 0, sb = 0;
-  size_t total() const { return ahat + bhat + t + sa + sb; }
-};
-BatchOzScratch batch_oz_scratch(const tmm::BatchProblem& d, int64_t tk, int slices) {
-  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-  BatchOzScratch r;
-  if (d.dtype == TMM_FLOAT) {
-    r.ahat = up((size_t)d.m * (size_t)tk * 8);
-    r.bhat = up((size_t)tk * (size_t)d.n * 8);
-    r.t = up((size_t)d.m * (size_t)d.n * 8);
-  }
-  r.sa = up(tmm::ozaki_split_bytes(d.m, tk, slices));
-  r.sb = up(tmm::ozaki_split_bytes(d.n, tk, slices));
-  return r;
+// the split views of problem position j of the plan for k tile kt
+void batch_oz_views(const tmm_context* ctx, const BatchOzPlan& plan, const tmm::BatchProblem& d, size_t j, int64_t kt,
+                    tmm::OzakiSplit* va, tmm::OzakiSplit* vb) {
+  char* arena = (char*)ctx->batch_oz_scratch.ptr + plan.arena_off;
+  const int64_t kk = std::min(plan.tk[j], d.k - kt * plan.tk[j]);
+  *va = tmm::ozaki_split_view(arena + plan.a_off[j], d.m, kk, plan.slices, ctx->oz_engine);
+  *vb = tmm::ozaki_split_view(arena + plan.b_off[j], d.n, kk, plan.slices, ctx->oz_engine);
 }
 
 int plan_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const std::vector<int>& ids,
                      BatchOzPlan* plan, bool* moved) {
   *plan = BatchOzPlan{};
+  *moved = false;
   if (ids.empty()) return TMM_SUCCESS;
-  plan->slices = batch_slices(ctx, TMM_DOUBLE);
-  plan->slices_f32 = batch_slices(ctx, TMM_FLOAT);
-  int branches = BATCH_OZ_BRANCHES;
-  if (const char* env = getenv("TMM_BATCH_OZ_BRANCHES")) branches = std::max(1, std::min(1024, atoi(env)));
-  const int nb = std::min<int>((int)ids.size(), branches);
-  plan->branch.assign((size_t)nb, {});
-  std::vector<double> load((size_t)nb, 0.0);
-  std::vector<size_t> need((size_t)nb, 0), work((size_t)nb, 0);
-  std::vector<int> order(ids);
-  auto cost = [&](int i) { return (double)dev[i].m * (double)dev[i].n * (double)dev[i].k; };
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+  BatchOzPlan& P = *plan;
+  P.ids = ids;
+  P.slices = batch_slices(ctx, TMM_DOUBLE);
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-  for (int id : order) {
-    const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    plan->branch[(size_t)b].push_back(id);
-    load[(size_t)b] += cost(id);
+  // arena: both operands' planes of every problem for one k tile
+  size_t arena = 0;
+  std::vector<double> cost;
+  for (int id : ids) {
     const tmm::BatchProblem& d = dev[(size_t)id];
     const int64_t tk = std::min<int64_t>(d.k, ctx->max_tile_k);
-    const bool f32 = d.dtype == TMM_FLOAT;
-    need[(size_t)b] = std::max(need[(size_t)b], batch_oz_scratch(d, tk, f32 ? plan->slices_f32 : plan->slices).total());
-    work[(size_t)b] = std::max(work[(size_t)b], up(tmm::ozaki_workspace_bytes_for(ctx->oz_engine, d.m, d.n)));
-    // per k tile: two two-kernel splits and the product (+ two embeddings and the combine for FP32)
-    plan->kernels += (f32 ? 8 : 5) * (int)((d.k + tk - 1) / tk);
+    P.tk.push_back(tk);
+    P.a_off.push_back(arena);
+    arena += up(tmm::ozaki_split_bytes(d.m, tk, P.slices));
+    P.b_off.push_back(arena);
+    arena += up(tmm::ozaki_split_bytes(d.n, tk, P.slices));
+    cost.push_back((double)d.m * (double)d.n * (double)d.k);
   }
-  size_t total = 0;
-  for (int b = 0; b < nb; ++b) {
-    plan->offset.push_back(total);
-    plan->work_bytes.push_back(work[(size_t)b]);
-    total += work[(size_t)b] + need[(size_t)b];
+  // chunks of about equal work, in problem order
+  const double total = std::accumulate(cost.begin(), cost.end(), 0.0);
+  const int nch = std::min<int>(BATCH_OZ_CHUNKS, (int)ids.size());
+  P.chunks.assign((size_t)nch, {});
+  double acc = 0.0;
+  for (size_t j = 0; j < ids.size(); ++j) {
+    const int c = std::min(nch - 1, (int)(acc / total * nch));
+    P.chunks[(size_t)c].push_back((int)j);
+    P.chunk_of.push_back(c);
+    acc += cost[j];
   }
+  P.work_off = 0;
+  const size_t work = up(tmm::ozaki_workspace_bytes(ctx->oz_engine));
+  P.arena_off = work;
+  P.arena_bytes = arena;
+  // the grouped launches' device records, per chunk and k-tile round
+  std::vector<unsigned char> images;
   void* before = ctx->batch_oz_scratch.ptr;
-  TMM_CUDA(ctx, ctx->batch_oz_scratch.reserve(total));
+  // the records hold device addresses inside the scratch: size it first, then build them
+  for (int pass = 0; pass < 2; ++pass) {
+    images.clear();
+    P.launches.clear();
+    P.kernels = 0;
+    for (int c = 0; c < nch; ++c) {
+      int rounds = 0;
+      for (int j : P.chunks[(size_t)c]) {
+        const tmm::BatchProblem& d = dev[(size_t)ids[(size_t)j]];
+        rounds = std::max<int>(rounds, (int)((d.k + P.tk[(size_t)j] - 1) / P.tk[(size_t)j]));
+      }
+      for (int r = 0; r < rounds; ++r) {
+        std::vector<tmm::GroupedProduct> prods;
+        for (int j : P.chunks[(size_t)c]) {
+          const tmm::BatchProblem& d = dev[(size_t)ids[(size_t)j]];
+          if ((int64_t)r * P.tk[(size_t)j] >= d.k) continue;
+          tmm::GroupedProduct g;
+          batch_oz_views(ctx, P, d, (size_t)j, r, &g.A, &g.B);
+          g.m = d.m;
+          g.n = d.n;
+          g.alpha = d.alpha;
+          g.beta = d.beta;
+          g.first_k_tile = r == 0;
+          g.C = (double*)d.c;
+          g.ldc = d.ldc;
+          prods.push_back(g);
+          P.kernels += 4;  // two two-kernel splits
+        }
+        BatchOzRound L{c, r, (int)prods.size(), 0, P.arena_off + P.arena_bytes + images.size()};
+        if (ctx->oz_engine == tmm::OZ_ENGINE_TCGEN05 && pass == 1) {
+          std::vector<unsigned char> img;
+          cudaError_t e = tmm::ozaki_tc_grouped_image(prods, (char*)ctx->batch_oz_scratch.ptr + P.arena_off,
+                                                      P.arena_bytes, img, &L.n_items);
+          if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki plan");
+          images.insert(images.end(), img.begin(), img.end());
+          images.resize(up(images.size()));
+        } else if (ctx->oz_engine == tmm::OZ_ENGINE_TCGEN05) {
+          // sizes only: records and tiles of this launch
+          size_t tiles = 0;
+          for (const auto& g : prods) tiles += (size_t)((g.m + 127) / 128) * (size_t)((g.n + 255) / 256);
+          images.resize(up(images.size() + up(prods.size() * 256) + tiles * 16));
+        }
+        P.kernels += ctx->oz_engine == tmm::OZ_ENGINE_TCGEN05 ? 1 : (int)prods.size();
+        P.launches.push_back(L);
+      }
+    }
+    if (pass == 0) TMM_CUDA(ctx, ctx->batch_oz_scratch.reserve(P.arena_off + P.arena_bytes + images.size() + 256));
+  }
+  *moved = ctx->batch_oz_scratch.ptr != before;
+  if (!images.empty())
+    TMM_CUDA(ctx, cudaMemcpy((char*)ctx->batch_oz_scratch.ptr + P.arena_off + P.arena_bytes, images.data(),
+                             images.size(), cudaMemcpyHostToDevice));
   void* wbefore = ctx->oz_work.ptr;
-  int st = reserve_oz_work(ctx, 0);  // the error word; workspaces live in the branch scratch
+  int st = reserve_oz_work(ctx, 0);  // the error word; the workspace is in the batch scratch
   if (st) return st;
-  *moved = ctx->batch_oz_scratch.ptr != before || ctx->oz_work.ptr != wbefore;
+  if (ctx->oz_work.ptr != wbefore) *moved = true;
   if (!ctx->oz_fork) TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->oz_fork, cudaEventDisableTiming));
-  while ((int)ctx->oz_branches.size() < nb) {
+  while (ctx->oz_branches.size() < 3) {  // copies in, splits and products, copies out
     cudaStream_t bs;
-    cudaEvent_t ev;
     TMM_CUDA(ctx, cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
     ctx->oz_branches.push_back(bs);
+  }
+  while (ctx->oz_branch_done.size() < 2 * (size_t)BATCH_OZ_CHUNKS + 2) {
+    cudaEvent_t ev;
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     ctx->oz_branch_done.push_back(ev);
   }
@@ -1542,114 +1609,199 @@ int copy_problem_out(tmm_context* ctx, const tmm_batch_problem& h, const tmm::Ba
   return TMM_SUCCESS;
 }
 
-// One FP32 problem of a batch on the Ozaki path, per k tile: the FP64 embedding of op(A) and
-// op(B), their digit planes, the engine's product T and C = alpha T + beta' C in double,
-// rounded once to float (beta' = beta on the first k tile, 1 after), as tmm_gemm does for a
-// float context on the Ozaki path.  alpha and beta are the problem's, rounded to float.
-int enqueue_batch_ozaki_f32(tmm_context* ctx, const tmm::BatchProblem& d, int64_t tk, int slices, char* base,
-                            double* work, cudaStream_t bs) {
-  const BatchOzScratch sc = batch_oz_scratch(d, tk, slices);
-  double* Ahat = (double*)base;
-  double* Bhat = (double*)(base + sc.ahat);
-  double* T = (double*)(base + sc.ahat + sc.bhat);
-  char* SA = base + sc.ahat + sc.bhat + sc.t;
-  char* SB = SA + sc.sa;
-  const float alpha = (float)d.alpha, beta = (float)d.beta, one = 1.f;
-  for (int64_t k0 = 0, kt = 0; k0 < d.k; k0 += tk, ++kt) {
-    const int64_t kk = std::min(tk, d.k - k0);
-    const float* ab = d.opa == tmm::OP_N ? (const float*)d.a + k0 * d.lda : (const float*)d.a + k0;
-    const float* bb = d.opb == tmm::OP_N ? (const float*)d.b + k0 : (const float*)d.b + k0 * d.ldb;
-    tmm::OzakiSplit va = tmm::ozaki_split_view(SA, d.m, kk, slices, ctx->oz_engine);
-    tmm::OzakiSplit vb = tmm::ozaki_split_view(SB, d.n, kk, slices, ctx->oz_engine);
-    cudaError_t e = tmm::ozaki_embed(TMM_FLOAT, ab, d.lda, d.opa, bb, d.ldb, d.opb, d.m, d.n, kk, Ahat, Bhat, bs);
-    if (e == cudaSuccess) e = tmm::ozaki_split(Ahat, d.m, tmm::OP_N, d.m, kk, va, bs);
-    if (e == cudaSuccess) e = tmm::ozaki_split(Bhat, kk, tmm::OP_T, d.n, kk, vb, bs);
-    if (e == cudaSuccess)
-      e = tmm::ozaki_gemm(va, vb, d.m, d.n, 1.0, 0.0, true, T, d.m, ctx->oz_engine, work, oz_error_word(ctx), bs);
-    if (e == cudaSuccess)
-      e = tmm::ozaki_combine(TMM_FLOAT, d.m, d.n, &alpha, kt == 0 ? &beta : &one, true, T, d.c, d.ldc, bs);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki launch");
-  }
-  return TMM_SUCCESS;
-}
-
-// Forks the branches from s and queues each branch's problems: with host operands
-// (host != nullptr) every problem copies its operands in on its branch right before its
-// split and its C out right after its product, so the host link overlaps the products of
-// the other branches.  join_batch_ozaki makes s wait for all branches.
+// Forks the pipeline's three streams from s and queues every chunk (see plan_batch_ozaki):
+// with host operands (host != nullptr) copies in, splits and products, copies out;
+// join_batch_ozaki makes s wait for the pipeline.
 int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const BatchOzPlan& plan,
                         cudaStream_t s, const tmm_batch_problem* host) {
-  if (plan.branch.empty()) return TMM_SUCCESS;
+  if (plan.ids.empty()) return TMM_SUCCESS;
+  cudaStream_t cin = ctx->oz_branches[1], comp = ctx->oz_branches[0], cout = ctx->oz_branches[2];
+  const size_t nch = plan.chunks.size();
+  cudaEvent_t* ev_in = &ctx->oz_branch_done[0];
+  cudaEvent_t* ev_done = &ctx->oz_branch_done[(size_t)BATCH_OZ_CHUNKS];
   TMM_CUDA(ctx, cudaEventRecord(ctx->oz_fork, s));
-  for (size_t b = 0; b < plan.branch.size(); ++b) {
-    cudaStream_t bs = ctx->oz_branches[b];
-    TMM_CUDA(ctx, cudaStreamWaitEvent(bs, ctx->oz_fork, 0));
-    double* work = (double*)((char*)ctx->batch_oz_scratch.ptr + plan.offset[b]);
-    char* base = (char*)ctx->batch_oz_scratch.ptr + plan.offset[b] + plan.work_bytes[b];
-    for (int id : plan.branch[b]) {
-      const tmm::BatchProblem& d = dev[(size_t)id];
-      if (host) {
-        int st = copy_problem_in(ctx, host[id], d, bs);
-        if (st) return st;
+  TMM_CUDA(ctx, cudaStreamWaitEvent(comp, ctx->oz_fork, 0));
+  if (host) {
+    TMM_CUDA(ctx, cudaStreamWaitEvent(cin, ctx->oz_fork, 0));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(cout, ctx->oz_fork, 0));
+  }
+  char* scratch = (char*)ctx->batch_oz_scratch.ptr;
+  double* work = (double*)(scratch + plan.work_off);
+  size_t li = 0;
+  for (size_t c = 0; c < nch; ++c) {
+    if (host) {
+      for (int j : plan.chunks[c]) {
+        const int id = plan.ids[(size_t)j];
+        if (int st = copy_problem_in(ctx, host[id], dev[(size_t)id], cin)) return st;
       }
-      const int64_t tk = std::min<int64_t>(d.k, ctx->max_tile_k);
-      if (d.dtype == TMM_FLOAT) {
-        int st = enqueue_batch_ozaki_f32(ctx, d, tk, plan.slices_f32, base, plan.work_bytes[b] ? work : nullptr, bs);
-        if (st) return st;
-        if (host && (st = copy_problem_out(ctx, host[id], d, bs))) return st;
-        continue;
-      }
-      const size_t sa_al = (tmm::ozaki_split_bytes(d.m, tk, plan.slices) + 255) / 256 * 256;
-      for (int64_t k0 = 0, kt = 0; k0 < d.k; k0 += tk, ++kt) {
-        const int64_t kk = std::min(tk, d.k - k0);
-        tmm::OzakiSplit va = tmm::ozaki_split_view(base, d.m, kk, plan.slices, ctx->oz_engine);
-        tmm::OzakiSplit vb = tmm::ozaki_split_view(base + sa_al, d.n, kk, plan.slices, ctx->oz_engine);
+      TMM_CUDA(ctx, cudaEventRecord(ev_in[c], cin));
+      TMM_CUDA(ctx, cudaStreamWaitEvent(comp, ev_in[c], 0));
+    }
+    for (; li < plan.launches.size() && plan.launches[li].chunk == (int)c; ++li) {
+      const BatchOzRound& L = plan.launches[li];
+      std::vector<std::pair<tmm::OzakiSplit, tmm::OzakiSplit>> views;
+      std::vector<int> pos;
+      for (int j : plan.chunks[c]) {
+        const tmm::BatchProblem& d = dev[(size_t)plan.ids[(size_t)j]];
+        const int64_t k0 = (int64_t)L.round * plan.tk[(size_t)j];
+        if (k0 >= d.k) continue;
+        tmm::OzakiSplit va, vb;
+        batch_oz_views(ctx, plan, d, (size_t)j, L.round, &va, &vb);
         const double* ab = d.opa == tmm::OP_N ? (const double*)d.a + k0 * d.lda : (const double*)d.a + k0;
         const double* bb = d.opb == tmm::OP_N ? (const double*)d.b + k0 : (const double*)d.b + k0 * d.ldb;
-        cudaError_t e = tmm::ozaki_split(ab, d.lda, d.opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, d.m, kk, va, bs);
-        if (e == cudaSuccess) e = tmm::ozaki_split(bb, d.ldb, d.opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, d.n, kk, vb, bs);
+        cudaError_t e = tmm::ozaki_split(ab, d.lda, d.opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, d.m, va.kk, va, comp);
         if (e == cudaSuccess)
-          e = tmm::ozaki_gemm(va, vb, d.m, d.n, d.alpha, d.beta, kt == 0, (double*)d.c, d.ldc, ctx->oz_engine,
-                              plan.work_bytes[b] ? work : nullptr, oz_error_word(ctx), bs);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki launch");
+          e = tmm::ozaki_split(bb, d.ldb, d.opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, d.n, vb.kk, vb, comp);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki split");
+        views.emplace_back(va, vb);
+        pos.push_back(j);
       }
-      if (host) {
-        int st = copy_problem_out(ctx, host[id], d, bs);
-        if (st) return st;
+      cudaError_t e = cudaSuccess;
+      if (ctx->oz_engine == tmm::OZ_ENGINE_TCGEN05) {
+        e = tmm::ozaki_gemm_tc_grouped(scratch + plan.arena_off, plan.arena_bytes, plan.slices, scratch + L.image_off,
+                                       L.n_probs, L.n_items, work, oz_error_word(ctx), comp);
+      } else {
+        for (size_t q = 0; q < views.size() && e == cudaSuccess; ++q) {
+          const tmm::BatchProblem& d = dev[(size_t)plan.ids[(size_t)pos[q]]];
+          e = tmm::ozaki_gemm(views[q].first, views[q].second, d.m, d.n, d.alpha, d.beta, L.round == 0, (double*)d.c,
+                              d.ldc, ctx->oz_engine, work, oz_error_word(ctx), comp);
+        }
+      }
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki launch");
+    }
+    TMM_CUDA(ctx, cudaEventRecord(ev_done[c], comp));
+    if (host) {
+      TMM_CUDA(ctx, cudaStreamWaitEvent(cout, ev_done[c], 0));
+      for (int j : plan.chunks[c]) {
+        const int id = plan.ids[(size_t)j];
+        if (int st = copy_problem_out(ctx, host[id], dev[(size_t)id], cout)) return st;
       }
     }
-    TMM_CUDA(ctx, cudaEventRecord(ctx->oz_branch_done[b], bs));
   }
   ctx->stats.kernels += plan.kernels;
   return TMM_SUCCESS;
 }
 
-int join_batch_ozaki(tmm_context* ctx, const BatchOzPlan& plan, cudaStream_t s) {
-  for (size_t b = 0; b < plan.branch.size(); ++b) TMM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->oz_branch_done[b], 0));
+int join_batch_ozaki(tmm_context* ctx, const BatchOzPlan& plan, cudaStream_t s, bool host) {
+  if (plan.ids.empty()) return TMM_SUCCESS;
+  cudaEvent_t* fin = &ctx->oz_branch_done[2 * (size_t)BATCH_OZ_CHUNKS];
+  TMM_CUDA(ctx, cudaEventRecord(fin[0], ctx->oz_branches[0]));
+  TMM_CUDA(ctx, cudaStreamWaitEvent(s, fin[0], 0));
+  if (host) {
+    TMM_CUDA(ctx, cudaEventRecord(fin[1], ctx->oz_branches[2]));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(s, fin[1], 0));
+    // the copy-in stream's last work precedes the compute stream's (it waited on it)
+  }
+  return TMM_SUCCESS;
+}
+
+// FP32 problems of a batch on the FP32 tensor-core engine: their bf16 planes (the whole k of
+// each problem) in one arena of the context's batch FP32 scratch, after its 256-byte error
+// word, and the grouped launch's records after the planes.
+struct BatchF32Plan {
+  std::vector<int> ids;
+  std::vector<size_t> a_off, b_off;  // plane offsets from the scratch base
+  size_t arena_off = 256, arena_bytes = 0, image_off = 0;
+  int n_probs = 0, n_items = 0;
+};
+
+int plan_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const std::vector<int>& ids,
+                   BatchF32Plan* plan, bool* moved) {
+  *plan = BatchF32Plan{};
+  *moved = false;
+  if (ids.empty()) return TMM_SUCCESS;
+  BatchF32Plan& P = *plan;
+  P.ids = ids;
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  size_t arena = 0;
+  std::vector<tmm::F32GroupedProduct> prods;
+  for (int id : ids) {
+    const tmm::BatchProblem& d = dev[(size_t)id];
+    P.a_off.push_back(P.arena_off + arena);
+    arena += up(tmm::f32tc_plane_bytes(d.m, d.k));
+    P.b_off.push_back(P.arena_off + arena);
+    arena += up(tmm::f32tc_plane_bytes(d.n, d.k));
+    prods.push_back(tmm::F32GroupedProduct{nullptr, nullptr, d.m, d.n, d.k, (float)d.alpha, (float)d.beta,
+                                           (float*)d.c, d.ldc});
+  }
+  P.arena_bytes = arena;
+  P.image_off = P.arena_off + arena;
+  const bool fresh = ctx->batch_f32_scratch.capacity < P.image_off + up(tmm::f32tc_grouped_image_bound(prods));
+  void* before = ctx->batch_f32_scratch.ptr;
+  TMM_CUDA(ctx, ctx->batch_f32_scratch.reserve(P.image_off + up(tmm::f32tc_grouped_image_bound(prods))));
+  if (fresh) TMM_CUDA(ctx, cudaMemset(ctx->batch_f32_scratch.ptr, 0, 256));  // the error word
+  *moved = ctx->batch_f32_scratch.ptr != before;
+  char* base = (char*)ctx->batch_f32_scratch.ptr;
+  for (size_t j = 0; j < prods.size(); ++j) {
+    prods[j].a_planes = base + P.a_off[j];
+    prods[j].b_planes = base + P.b_off[j];
+  }
+  std::vector<unsigned char> img;
+  cudaError_t e = tmm::f32tc_grouped_image(prods, base + P.arena_off, P.arena_bytes, img, &P.n_items);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched FP32 plan");
+  P.n_probs = (int)prods.size();
+  if (!img.empty()) TMM_CUDA(ctx, cudaMemcpy(base + P.image_off, img.data(), img.size(), cudaMemcpyHostToDevice));
+  TMM_CUDA(ctx, tmm::f32tc_prepare());
+  return TMM_SUCCESS;
+}
+
+// splits and the grouped launch on stream t (operands already in place)
+int enqueue_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const BatchF32Plan& P,
+                      cudaStream_t t) {
+  if (P.ids.empty()) return TMM_SUCCESS;
+  char* base = (char*)ctx->batch_f32_scratch.ptr;
+  for (size_t j = 0; j < P.ids.size(); ++j) {
+    const tmm::BatchProblem& d = dev[(size_t)P.ids[j]];
+    // lines of op(A): its rows (adjacent when A is not transposed); of op(B): its columns
+    cudaError_t e = tmm::f32tc_split_lines((const float*)d.a, d.lda, d.opa == tmm::OP_N, d.m, d.k, base + P.a_off[j], t);
+    if (e == cudaSuccess)
+      e = tmm::f32tc_split_lines((const float*)d.b, d.ldb, d.opb != tmm::OP_N, d.n, d.k, base + P.b_off[j], t);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched FP32 split");
+  }
+  cudaError_t e = tmm::f32tc_gemm_grouped(base + P.arena_off, P.arena_bytes, base + P.image_off, P.n_probs, P.n_items,
+                                          (int*)base, t);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched FP32 launch");
+  ctx->stats.kernels += 2 * P.ids.size() + 1;
+  return TMM_SUCCESS;
+}
+
+// the FP32 problems' work on the batch's second stream, forked from and joined into s
+int fork_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const BatchF32Plan& P, cudaStream_t s,
+                   bool join) {
+  if (P.ids.empty()) return TMM_SUCCESS;
+  if (!join) {
+    TMM_CUDA(ctx, cudaEventRecord(ctx->batch_f32_fork, s));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->batch_f32_stream, ctx->batch_f32_fork, 0));
+    return enqueue_batch_f32(ctx, dev, P, ctx->batch_f32_stream);
+  }
+  TMM_CUDA(ctx, cudaEventRecord(ctx->batch_f32_join, ctx->batch_f32_stream));
+  TMM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->batch_f32_join, 0));
   return TMM_SUCCESS;
 }
 
 // copies in, the persistent launch, copies out (host operands)
 int enqueue_batch(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const tmm_batch_problem* host,
-                  int count, int n_work, int n_f64, int any_k0, const BatchOzPlan& oz, cudaStream_t s) {
+                  int count, int n_work, int n_f64, int any_k0, const BatchOzPlan& oz, const BatchF32Plan& f32,
+                  cudaStream_t s) {
   const size_t rec = tmm::batch_problem_record_bytes();
   const void* dprobs = ctx->batch_meta.ptr;
   const void* dwork = (const char*)ctx->batch_meta.ptr + (rec * (size_t)count + 255) / 256 * 256;
   std::vector<char> on_branch((size_t)count, 0);
-  for (const auto& br : oz.branch)
-    for (int id : br) on_branch[(size_t)id] = 1;
+  for (int id : oz.ids) on_branch[(size_t)id] = 1;
   // the Ozaki branches first: they move their own operands
   int st = enqueue_batch_ozaki(ctx, dev, oz, s, host);
   if (st) return st;
   for (int i = 0; i < count; ++i)
     if (!on_branch[(size_t)i] && (st = copy_problem_in(ctx, host[i], dev[i], s))) return st;
+  if ((st = fork_batch_f32(ctx, dev, f32, s, false))) return st;
   cudaError_t e = tmm::batch_launch(dprobs, count, dwork, n_f64, n_work - n_f64, any_k0, s, ctx->batch_aux,
                                     ctx->batch_fork, ctx->batch_join);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
   ctx->stats.kernels += (n_f64 > 0) + (n_work - n_f64 > 0) + (any_k0 ? 1 : 0);
+  if ((st = fork_batch_f32(ctx, dev, f32, s, true))) return st;
   for (int i = 0; i < count; ++i)
     if (!on_branch[(size_t)i] && (st = copy_problem_out(ctx, host[i], dev[i], s))) return st;
-  return join_batch_ozaki(ctx, oz, s);
+  return join_batch_ozaki(ctx, oz, s, true);
 }
 
 }  // namespace
@@ -1721,19 +1873,30 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
     }
   }
   // on the Ozaki path FP64 problems with k > 0 leave the grouped kernels' list (their records
-  // stay, empty) for per-problem engine launches on branch streams
-  std::vector<int> oz_ids;
+  // stay, empty) for the engine's grouped launches
+  std::vector<int> oz_ids, f32_ids;
   std::vector<tmm::BatchProblem> grouped = dev;
-  // FP32 problems join with TMM_BATCH_OZ_F32=1: beside the Ozaki branches the grouped FP32
-  // kernel was faster (512 problems: 76.9 ms per call against 84.2 ms with them on the engine)
-  const char* f32_env = getenv("TMM_BATCH_OZ_F32");
-  const bool f32_on_engine = f32_env && f32_env[0] == '1';
   if (ctx->path == TMM_PATH_OZAKI)
     for (int i = 0; i < count; ++i)
-      if (dev[i].m > 0 && dev[i].n > 0 && dev[i].k > 0 && (dev[i].dtype == TMM_DOUBLE || f32_on_engine)) {
+      if (dev[i].m > 0 && dev[i].n > 0 && dev[i].k > 0 && dev[i].dtype == TMM_DOUBLE) {
         oz_ids.push_back(i);
         grouped[i].m = grouped[i].n = 0;
       }
+  // FP32 problems with k > 0 run on the FP32 tensor-core engine in one grouped launch
+  // (TMM_F32_KERNEL=simt: the grouped FFMA kernel)
+  if (!ctx->f32_simt)
+    for (int i = 0; i < count; ++i)
+      if (dev[i].m > 0 && dev[i].n > 0 && dev[i].k > 0 && dev[i].dtype == TMM_FLOAT) {
+        f32_ids.push_back(i);
+        grouped[i].m = grouped[i].n = 0;
+      }
+  BatchF32Plan f32;
+  {
+    bool moved = false;
+    int st0 = plan_batch_f32(ctx, dev, f32_ids, &f32, &moved);
+    if (st0) return st0;
+    if (moved) drop_batch_graph(ctx);
+  }
   BatchOzPlan oz;
   {
     bool moved = false;
@@ -1749,7 +1912,13 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_fork, cudaEventDisableTiming));
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_join, cudaEventDisableTiming));
   }
-  const int kernels = (n_f64 > 0) + (n_work - n_f64 > 0) + any_k0 + oz.kernels;
+  if (!ctx->batch_f32_stream) {
+    TMM_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->batch_f32_stream, cudaStreamNonBlocking));
+    TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_f32_fork, cudaEventDisableTiming));
+    TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_f32_join, cudaEventDisableTiming));
+  }
+  const int kernels = (n_f64 > 0) + (n_work - n_f64 > 0) + any_k0 + oz.kernels +
+                      (f32.ids.empty() ? 0 : 2 * (int)f32.ids.size() + 1);
   const size_t pb_al = (pb.size() + 255) / 256 * 256;
   {
     void* before = ctx->batch_meta.ptr;
@@ -1759,7 +1928,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
   // the layout key: every field of every problem, plus the chosen variants
   std::vector<unsigned char> key((const unsigned char*)probs, (const unsigned char*)probs + sizeof(tmm_batch_problem) * count);
   for (auto& d : dev) key.push_back((unsigned char)d.variant);
-  for (int v : {ctx->path, oz.slices, oz.slices_f32, ctx->oz_engine, ctx->max_tile_k, (int)f32_on_engine}) {
+  for (int v : {ctx->path, oz.slices, ctx->oz_engine, ctx->max_tile_k, (int)ctx->f32_simt}) {
     const unsigned char* vb = (const unsigned char*)&v;
     key.insert(key.end(), vb, vb + sizeof(v));
   }
@@ -1782,10 +1951,12 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
     if (device_operands) {
       st = enqueue_batch_ozaki(ctx, dev, oz, s, nullptr);
       if (st) return st;
+      if ((st = fork_batch_f32(ctx, dev, f32, s, false))) return st;
       cudaError_t e = tmm::batch_launch(ctx->batch_meta.ptr, count, (char*)ctx->batch_meta.ptr + pb_al, n_f64,
                                         n_work - n_f64, any_k0, s, ctx->batch_aux, ctx->batch_fork, ctx->batch_join);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
-      st = join_batch_ozaki(ctx, oz, s);
+      if ((st = fork_batch_f32(ctx, dev, f32, s, true))) return st;
+      st = join_batch_ozaki(ctx, oz, s, false);
       if (st) return st;
       ctx->stats.kernels = kernels;
     } else {
@@ -1798,7 +1969,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
       if (pinned) {
         drop_batch_graph(ctx);
         TMM_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, oz, s);
+        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, oz, f32, s);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(s, &graph);
         if (st) {
@@ -1816,7 +1987,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
         TMM_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
         ctx->stats.batch_graph = 1;
       } else {
-        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, oz, s);
+        st = enqueue_batch(ctx, dev, probs, count, n_work, n_f64, any_k0, oz, f32, s);
         if (st) return st;
       }
     }
@@ -1827,6 +1998,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
     ctx->stats.ozaki_slices = oz.slices;
     st = check_oz_error(ctx);
   }
+  if (!st && !f32_ids.empty()) st = check_f32_error(ctx);
   ctx->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return st;
 }

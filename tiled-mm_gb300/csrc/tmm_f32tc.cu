@@ -33,7 +33,10 @@
 #include <cudaTypedefs.h>
 
 #include <cstdlib>
+#include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "tmm_f32tc.h"
 #include "tmm_tc_ptx.cuh"
@@ -95,6 +98,64 @@ struct Params {
   int* err;
   int tiles_m, tiles_n;
 };
+
+// A product of a grouped launch (f32tc_gemm_grouped): its planes start at 128-byte row
+// a_row0 / b_row0 of the launch's one tensor map over the arena of all products' planes.
+struct GroupProblem {
+  int64_t a_row0, b_row0, a_rows_pad, b_rows_pad;
+  float* C;
+  int64_t ldc, m, n;
+  float alpha, beta;
+  int nkb, pad;
+};
+struct GroupArgs {
+  const GroupProblem* probs;
+  const int4* items;  // (problem, 128-row tile, 256-column tile, unused)
+  int n_items;
+};
+
+// A tile of a launch and its product's geometry and epilogue operands.
+struct Job {
+  int tm, tn, nkb;
+  int64_t a_row0, b_row0, a_rows_pad, b_rows_pad;
+  float* C;
+  int64_t ldc, m, n;
+  float alpha, beta;
+};
+template <bool GROUPED>
+__device__ __forceinline__ Job job_of(int ct, const Params& P, const GroupArgs& G) {
+  Job j;
+  if (GROUPED) {
+    const int4 it = G.items[ct];
+    const GroupProblem& q = G.probs[it.x];
+    j.tm = it.y;
+    j.tn = it.z;
+    j.nkb = q.nkb;
+    j.a_row0 = q.a_row0;
+    j.b_row0 = q.b_row0;
+    j.a_rows_pad = q.a_rows_pad;
+    j.b_rows_pad = q.b_rows_pad;
+    j.C = q.C;
+    j.ldc = q.ldc;
+    j.m = q.m;
+    j.n = q.n;
+    j.alpha = q.alpha;
+    j.beta = q.beta;
+  } else {
+    tile_coords(ct, P.tiles_m, P.tiles_n, GROUP_M, &j.tm, &j.tn);
+    j.nkb = P.nkb;
+    j.a_row0 = j.b_row0 = 0;
+    j.a_rows_pad = P.a_rows_pad;
+    j.b_rows_pad = P.b_rows_pad;
+    j.C = P.C;
+    j.ldc = P.ldc;
+    j.m = P.m;
+    j.n = P.n;
+    j.alpha = P.alpha;
+    j.beta = P.beta;
+  }
+  return j;
+}
 
 // ------------------------------------------------------------------ split: FP32 -> 3 bf16 planes
 constexpr int SPL = 64, SP_THREADS = 256;
@@ -159,8 +220,10 @@ f32tc_split_kernel(const float* __restrict__ X, int64_t ld, int64_t rows, int64_
 }
 
 // ------------------------------------------------------------------ GEMM
+template <bool GROUPED>
 __global__ void __launch_bounds__(THREADS, 1)
-f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
+f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P,
+                  const GroupArgs G) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = (uint64_t*)(smem + (size_t)STAGES * STAGE_BYTES);
@@ -170,8 +233,7 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
-  const int total_tiles = P.tiles_m * P.tiles_n;
-  const int steps = NPAIRS * P.nkb;  // k-blocks per tile
+  const int total_tiles = GROUPED ? G.n_items : P.tiles_m * P.tiles_n;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -202,20 +264,22 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t phase = 0;
       bool ok = true;
       for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
-        int tm, tn;
-        tile_coords(ct, P.tiles_m, P.tiles_n, GROUP_M, &tm, &tn);
+        const Job J = job_of<GROUPED>(ct, P, G);
+        const int steps = NPAIRS * J.nkb;  // k-blocks of this tile
         for (int t = 0; t < steps && ok; ++t) {
-          const int pr = t / P.nkb, kb = t - pr * P.nkb;
+          const int pr = t / J.nkb, kb = t - pr * J.nkb;
           ok = mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err);
           if (!ok) break;
           const uint32_t fb = full0 + 8 * stage;
           mbar_expect_tx(fb, STAGE_BYTES);
           uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
-          tma_load_2d(smem_u32(sa), &tmA, 0, box_y(pair_a(pr), (int64_t)tm * BM, kb, P.a_rows_pad, P.nkb), fb);
+          tma_load_2d(smem_u32(sa), &tmA, 0,
+                      (int)(J.a_row0 + box_y(pair_a(pr), (int64_t)J.tm * BM, kb, J.a_rows_pad, J.nkb)), fb);
 #pragma unroll
           for (int j = 0; j < BN / LINE_BLOCK; ++j)
             tma_load_2d(smem_u32(sa + A_BYTES + j * LINE_BLOCK * KBYTES), &tmB, 0,
-                        box_y(pair_b(pr), (int64_t)tn * BN + j * LINE_BLOCK, kb, P.b_rows_pad, P.nkb), fb);
+                        (int)(J.b_row0 + box_y(pair_b(pr), (int64_t)J.tn * BN + j * LINE_BLOCK, kb, J.b_rows_pad,
+                                               J.nkb)), fb);
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
@@ -241,6 +305,7 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t phase = 0, tph = 0;  // tph bit b: phase of accumulator b's full barrier
       bool ok = true;
       for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
+        const int steps = NPAIRS * (GROUPED ? G.probs[G.items[ct].x].nkb : P.nkb);
         // the accumulator is free once the epilogue has drained its previous tile
         ok = mbar_wait(tempty0 + 8 * buf, ((tph >> buf) & 1u) ^ 1u, abort_flag, P.err);
         if (!ok) break;
@@ -280,8 +345,7 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint32_t tphase[2] = {0, 0};
     int buf = 0;
     for (int ct = blockIdx.x; ct < total_tiles; ct += gridDim.x) {
-      int tm, tn;
-      tile_coords(ct, P.tiles_m, P.tiles_n, GROUP_M, &tm, &tn);
+      const Job J = job_of<GROUPED>(ct, P, G);
       int okw = 1;
       if (lane == 0) okw = mbar_wait(tfull0 + 8 * buf, tphase[buf], abort_flag, P.err, EPI_WAIT_HINT_NS) ? 1 : 0;
       const bool ok = __shfl_sync(0xffffffffu, okw, 0) != 0;
@@ -289,9 +353,9 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       if (!ok) break;
       tc_fence_after();
       const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
-      const int64_t gi = (int64_t)tm * BM + row;
-      const bool row_ok = gi < P.m;
-      const bool read_c = P.beta != 0.0f;
+      const int64_t gi = (int64_t)J.tm * BM + row;
+      const bool row_ok = gi < J.m;
+      const bool read_c = J.beta != 0.0f;
 #pragma unroll 1
       for (int c = 0; c < BN / 32; ++c) {
         uint32_t r[32];
@@ -302,16 +366,16 @@ f32tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
           __syncwarp();
           if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
         }
-        const int64_t gj0 = (int64_t)tn * BN + c * 32;
-        if (!row_ok || gj0 >= P.n) continue;
-        const int nv = P.n - gj0 < 32 ? (int)(P.n - gj0) : 32;
-        float* cp = P.C + gi + gj0 * P.ldc;
+        const int64_t gj0 = (int64_t)J.tn * BN + c * 32;
+        if (!row_ok || gj0 >= J.n) continue;
+        const int nv = J.n - gj0 < 32 ? (int)(J.n - gj0) : 32;
+        float* cp = J.C + gi + gj0 * J.ldc;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           if (j >= nv) break;
           const float acc = __uint_as_float(r[j]);
-          float* q = cp + (int64_t)j * P.ldc;
-          *q = read_c ? fmaf(P.alpha, acc, P.beta * *q) : P.alpha * acc;
+          float* q = cp + (int64_t)j * J.ldc;
+          *q = read_c ? fmaf(J.alpha, acc, J.beta * *q) : J.alpha * acc;
         }
       }
       tphase[buf] ^= 1;
@@ -372,7 +436,9 @@ const DeviceSetup* device_setup() {
     d.status = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     if (d.status != cudaSuccess) return;
     if (d.sms <= 0) d.sms = 1;
-    d.status = cudaFuncSetAttribute(f32tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    d.status = cudaFuncSetAttribute(f32tc_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (d.status != cudaSuccess) return;
+    d.status = cudaFuncSetAttribute(f32tc_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
   });
   return &d;
 }
@@ -384,6 +450,102 @@ size_t plane_bytes(int64_t lines, int64_t kk) {
 }
 
 }  // namespace f32tc
+
+size_t f32tc_plane_bytes(int64_t lines, int64_t k) { return f32tc::plane_bytes(lines, k); }
+
+cudaError_t f32tc_split_lines(const float* X, int64_t ld, bool lines_contiguous, int64_t lines, int64_t k,
+                              void* planes, cudaStream_t s) {
+  using namespace f32tc;
+  if (lines <= 0 || k <= 0) return cudaSuccess;
+  const int64_t rows_pad = round_up(lines, 256), k_pad = round_up(k, KE);
+  if (k_pad / SPL > 65535) return cudaErrorInvalidValue;
+  const dim3 g((unsigned)(rows_pad / SPL), (unsigned)(k_pad / SPL));
+  if (lines_contiguous)
+    f32tc_split_kernel<0><<<g, SP_THREADS, 0, s>>>(X, ld, lines, k, (__nv_bfloat16*)planes, rows_pad, k_pad);
+  else
+    f32tc_split_kernel<1><<<g, SP_THREADS, 0, s>>>(X, ld, lines, k, (__nv_bfloat16*)planes, rows_pad, k_pad);
+  return cudaGetLastError();
+}
+
+cudaError_t f32tc_grouped_image(const std::vector<F32GroupedProduct>& prods, const void* arena, size_t arena_bytes,
+                                std::vector<unsigned char>& out, int* n_items) {
+  using namespace f32tc;
+  std::vector<GroupProblem> recs;
+  std::vector<int4> items;
+  std::vector<int64_t> cost;
+  for (const F32GroupedProduct& p : prods) {
+    if (p.m <= 0 || p.n <= 0 || p.k <= 0) continue;
+    const int64_t aoff = (const char*)p.a_planes - (const char*)arena, boff = (const char*)p.b_planes - (const char*)arena;
+    if (aoff < 0 || boff < 0 || aoff % KBYTES || boff % KBYTES) return cudaErrorInvalidValue;
+    // every box of the planes lies inside the arena that the launch's tensor map covers
+    if ((size_t)aoff + plane_bytes(p.m, p.k) > arena_bytes || (size_t)boff + plane_bytes(p.n, p.k) > arena_bytes)
+      return cudaErrorInvalidValue;
+    GroupProblem r;
+    r.a_row0 = aoff / KBYTES;
+    r.b_row0 = boff / KBYTES;
+    r.a_rows_pad = round_up(p.m, 256);
+    r.b_rows_pad = round_up(p.n, 256);
+    r.C = p.C;
+    r.ldc = p.ldc;
+    r.m = p.m;
+    r.n = p.n;
+    r.alpha = p.alpha;
+    r.beta = p.beta;
+    r.nkb = (int)(round_up(p.k, KE) / KE);
+    r.pad = 0;
+    const int idx = (int)recs.size();
+    recs.push_back(r);
+    for (int tm = 0; tm < (int)((p.m + BM - 1) / BM); ++tm)
+      for (int tn = 0; tn < (int)((p.n + BN - 1) / BN); ++tn) {
+        items.push_back(make_int4(idx, tm, tn, 0));
+        cost.push_back((int64_t)r.nkb);
+      }
+  }
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+  const size_t rec_bytes = (recs.size() * sizeof(GroupProblem) + 255) / 256 * 256;
+  out.assign(rec_bytes + items.size() * sizeof(int4), 0);
+  if (!recs.empty()) memcpy(out.data(), recs.data(), recs.size() * sizeof(GroupProblem));
+  int4* it = (int4*)(out.data() + rec_bytes);
+  for (size_t i = 0; i < order.size(); ++i) it[i] = items[order[i]];
+  *n_items = (int)items.size();
+  return cudaSuccess;
+}
+
+size_t f32tc_grouped_image_bound(const std::vector<F32GroupedProduct>& prods) {
+  size_t tiles = 0;
+  for (const auto& p : prods) tiles += (size_t)((p.m + 127) / 128) * (size_t)((p.n + 255) / 256);
+  return (prods.size() * sizeof(f32tc::GroupProblem) + 255) / 256 * 256 + tiles * sizeof(int4);
+}
+
+cudaError_t f32tc_gemm_grouped(const void* arena, size_t arena_bytes, const void* dev_image, int n_probs, int n_items,
+                               int* err, cudaStream_t s) {
+  using namespace f32tc;
+  if (n_items <= 0) return cudaSuccess;
+  if (!arena || !dev_image || !err || arena_bytes / KBYTES > (size_t)INT32_MAX) return cudaErrorInvalidValue;
+  const DeviceSetup* d = device_setup();
+  if (!d) return cudaErrorInvalidDevice;
+  if (d->status != cudaSuccess) return d->status;
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  CUtensorMap map;
+  cuuint64_t dims[2] = {(cuuint64_t)KBYTES, (cuuint64_t)(arena_bytes / KBYTES)};
+  cuuint64_t strides[1] = {(cuuint64_t)KBYTES};
+  cuuint32_t box[2] = {(cuuint32_t)KBYTES, (cuuint32_t)LINE_BLOCK};
+  cuuint32_t estr[2] = {1, 1};
+  if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(arena), dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  Params P{};
+  P.err = err;
+  const size_t rec_bytes = ((size_t)n_probs * sizeof(GroupProblem) + 255) / 256 * 256;
+  const GroupArgs G{(const GroupProblem*)dev_image, (const int4*)((const char*)dev_image + rec_bytes), n_items};
+  const int ctas = n_items < d->sms ? n_items : d->sms;
+  f32tc_gemm_kernel<true><<<ctas, THREADS, SMEM_BYTES, s>>>(map, map, P, G);
+  return cudaGetLastError();
+}
 
 size_t f32tc_scratch_bytes(int64_t m, int64_t n, int64_t k) {
   return 256 + f32tc::plane_bytes(m, k) + f32tc::plane_bytes(n, k);
@@ -439,7 +601,7 @@ cudaError_t f32tc_gemm(Op opa, Op opb, int64_t m, int64_t n, int64_t k, float al
   P.tiles_n = (int)((n + BN - 1) / BN);
   const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
   const int ctas = tiles < d->sms ? (int)tiles : d->sms;
-  f32tc_gemm_kernel<<<ctas, THREADS, SMEM_BYTES, s>>>(ma, mb, P);
+  f32tc_gemm_kernel<false><<<ctas, THREADS, SMEM_BYTES, s>>>(ma, mb, P, GroupArgs{nullptr, nullptr, 0});
   return cudaGetLastError();
 }
 

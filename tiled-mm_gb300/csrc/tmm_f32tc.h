@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "tmm_kernels.h"
 
 namespace tmm {
@@ -18,6 +20,30 @@ cudaError_t f32tc_prepare();
 cudaError_t f32tc_gemm(Op opa, Op opb, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
                        const float* B, int64_t ldb, float beta, float* C, int64_t ldc, void* scratch,
                        size_t scratch_bytes, cudaStream_t s);
+
+// Grouped form (a batch's FP32 problems): every product's bf16 planes live in one arena
+// (f32tc_plane_bytes per operand; offsets multiples of 256 bytes), written by
+// f32tc_split_lines (lines of op(A) are its rows, lines of op(B) its columns;
+// lines_contiguous: consecutive lines are adjacent in memory, i.e. element (line, l) at
+// X[line + l ld], else at X[l + line ld]); f32tc_grouped_image writes the launch's device
+// records (at most f32tc_grouped_image_bound bytes), to be copied to dev_image, and
+// f32tc_gemm_grouped multiplies all products in one persistent launch.
+struct F32GroupedProduct {
+  const void* a_planes;
+  const void* b_planes;
+  int64_t m, n, k;
+  float alpha, beta;
+  float* C;
+  int64_t ldc;
+};
+size_t f32tc_plane_bytes(int64_t lines, int64_t k);
+cudaError_t f32tc_split_lines(const float* X, int64_t ld, bool lines_contiguous, int64_t lines, int64_t k,
+                              void* planes, cudaStream_t s);
+cudaError_t f32tc_grouped_image(const std::vector<F32GroupedProduct>& prods, const void* arena, size_t arena_bytes,
+                                std::vector<unsigned char>& out, int* n_items);
+size_t f32tc_grouped_image_bound(const std::vector<F32GroupedProduct>& prods);
+cudaError_t f32tc_gemm_grouped(const void* arena, size_t arena_bytes, const void* dev_image, int n_probs, int n_items,
+                               int* err, cudaStream_t s);
 
 // Complex float through the real embedding on this engine (tmm_ozaki_embed.cu): Ahat
 // (2m x 2k, ld 2m) and Bhat (2k x n, ld 2k) in float, conjugating for op 'C'; after the engine

@@ -8,6 +8,8 @@
 // the algorithm and its published sources.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <vector>
 #include <stdint.h>
 
 #include "tmm_c_api.h"
@@ -118,5 +120,25 @@ int64_t ozaki_tc_pass_blocks();
 int ozaki_tc_k_block();
 cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
                           bool first_k_tile, double* C, int64_t ldc, double* work, int* err, cudaStream_t s);
+
+// One persistent launch over the tiles of several products (a batch's FP64 problems on the
+// Ozaki path): product i multiplies the split planes A, B (tcgen05 blocked layout, the same
+// slice count, all inside one arena) into C with its own alpha, beta and first-k-tile flag,
+// exactly as ozaki_gemm_tc would on its own.  ozaki_tc_grouped_image writes the launch's
+// device records (problems, then the tile list, largest problems first) into out, to be
+// copied to device memory at dev_image; ozaki_gemm_tc_grouped launches on them.  work:
+// ozaki_tc_workspace_bytes() bytes.
+struct GroupedProduct {
+  OzakiSplit A, B;
+  int64_t m, n;
+  double alpha, beta;
+  bool first_k_tile;
+  double* C;
+  int64_t ldc;
+};
+cudaError_t ozaki_tc_grouped_image(const std::vector<GroupedProduct>& prods, const void* arena, size_t arena_bytes,
+                                   std::vector<unsigned char>& out, int* n_items);
+cudaError_t ozaki_gemm_tc_grouped(const void* arena, size_t arena_bytes, int slices, const void* dev_image, int n_probs,
+                                  int n_items, double* work, int* err, cudaStream_t s);
 
 }  // namespace tmm

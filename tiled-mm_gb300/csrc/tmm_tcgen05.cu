@@ -30,10 +30,12 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "tmm_ozaki.h"
 #include "tmm_tc_ptx.cuh"
@@ -107,21 +109,30 @@ struct Seq {
 };
 
 // Position of the MMA issuer in its (tile, sequence) order: tiles ct, ct + stride, ...
+// nkb_of(ct) gives tile ct's k-blocks; the next tile's count is read when a tile starts, so
+// that a lookup in global memory (grouped launches) is not waited on at the tile change.
 struct MmaCursor {
   Seq q;
   int ct;
+  int nkb_next;
   bool valid;
-  __device__ void start(int ct0, int total, int s, int nkb) {
+  template <typename NkbOf>
+  __device__ void start(int ct0, int stride, int total, int s, NkbOf nkb_of) {
     ct = ct0;
     valid = ct < total;
-    q.start(s, nkb);
+    q.start(s, valid ? nkb_of(ct) : 1);
+    nkb_next = ct + stride < total ? nkb_of(ct + stride) : 1;
   }
-  __device__ void next(int stride, int total, int s, int nkb) {
+  template <typename NkbOf>
+  __device__ void next(int stride, int total, int s, NkbOf nkb_of) {
     q.next();
     if (q.done()) {
       ct += stride;
       valid = ct < total;
-      if (valid) q.start(s, nkb);
+      if (valid) {
+        q.start(s, nkb_next);
+        nkb_next = ct + stride < total ? nkb_of(ct + stride) : 1;
+      }
     }
   }
 };
@@ -203,6 +214,38 @@ __device__ __forceinline__ void pace_gate(const Params& P, unsigned long long c,
 // a producer that has issued all its work lifts its weight off the others' gates
 constexpr unsigned long long PACE_DONE = 1ull << 40;
 
+// What the epilogue of a tile needs: its problem's exponents, sizes, scalars and C.
+struct Epi {
+  const int32_t* ea;
+  const int32_t* eb;
+  int64_t m, n;
+  double alpha, beta;
+  int first;
+  double* C;
+  int64_t ldc;
+};
+__device__ __forceinline__ Epi epi_of(const Params& P) {
+  return Epi{P.ea, P.eb, P.m, P.n, P.alpha, P.beta, P.first, P.C, P.ldc};
+}
+
+// A problem of a grouped launch (ozaki_gemm_tc_grouped): its digit planes start at row
+// a_row0 / b_row0 of the launch's tensor maps (one map over all problems' A planes, one
+// over all B planes, in 128-byte rows).
+struct GroupProblem {
+  int64_t a_row0, b_row0, a_rows_pad, b_rows_pad;
+  const int32_t* ea;
+  const int32_t* eb;
+  double* C;
+  int64_t ldc, m, n;
+  double alpha, beta;
+  int nkb, first;
+};
+struct GroupArgs {
+  const GroupProblem* probs;
+  const int4* items;  // (problem, 128-row tile index, 256-column tile index, unused)
+  int n_items;
+};
+
 // FP64 arithmetic issues at about two operations per clock and SM on this GPU, so the
 // exact steps of the drain run on the integer pipes:
 // the pass sum S is an integer-valued FP32 (|S| < 2^24, exact by the pass limit), and
@@ -233,7 +276,7 @@ __device__ __forceinline__ double scalbn_fast(double x, int n) {
 // C values are issued together.  One FP64 add per element and pass (none on the first).
 template <typename Release>
 __device__ __forceinline__ void drain_pass(uint32_t tbase, double* __restrict__ slot, int row, int g, bool first_pass,
-                                           bool last, const Params& P, int64_t gi, int64_t col0, Release release) {
+                                           bool last, const Epi& P, int64_t gi, int64_t col0, Release release) {
   const int sh = OZ_DIGIT_BITS * g;
   const bool row_ok = gi < P.m;
   const int ei = last && row_ok ? P.ea[gi] : 0;
@@ -291,11 +334,51 @@ __device__ __forceinline__ void drain_pass(uint32_t tbase, double* __restrict__ 
   }
 }
 
+// A tile of a launch: its coordinates, its problem's k-blocks and plane geometry.  A plain
+// launch walks the tiles of one product in band order; a grouped launch walks a work list of
+// (problem, tile) items of many products whose planes share one tensor map per operand.
+struct Job {
+  int tm, tn, nkb;
+  int64_t a_row0, b_row0, a_rows_pad, b_rows_pad;
+};
+template <bool GROUPED>
+__device__ __forceinline__ Job job_of(int ct, const Params& P, const GroupArgs& G, int group) {
+  Job j;
+  if (GROUPED) {
+    const int4 it = G.items[ct];
+    const GroupProblem& q = G.probs[it.x];
+    j.tm = it.y;
+    j.tn = it.z;
+    j.nkb = q.nkb;
+    j.a_row0 = q.a_row0;
+    j.b_row0 = q.b_row0;
+    j.a_rows_pad = q.a_rows_pad;
+    j.b_rows_pad = q.b_rows_pad;
+  } else {
+    tile_coords(ct, P.tiles_m, P.tiles_n, group, &j.tm, &j.tn);
+    j.nkb = P.nkb;
+    j.a_row0 = j.b_row0 = 0;
+    j.a_rows_pad = P.a_rows_pad;
+    j.b_rows_pad = P.b_rows_pad;
+  }
+  return j;
+}
+template <bool GROUPED>
+__device__ __forceinline__ Epi epi_job(int ct, const Params& P, const GroupArgs& G) {
+  if (!GROUPED) return epi_of(P);
+  const GroupProblem& q = G.probs[G.items[ct].x];
+  return Epi{q.ea, q.eb, q.m, q.n, q.alpha, q.beta, q.first, q.C, q.ldc};
+}
+
 // One CTA per SM computes its 128 x 256 tiles alone: every TMA copy lands in
 // this CTA's own shared memory (no cluster, no multicast), and a stage is
-// refilled once this CTA's MMAs have read it.
+// refilled once this CTA's MMAs have read it.  GROUPED: the tiles are the items of a
+// work list over several products (ozaki_gemm_tc_grouped), each with its own k-blocks,
+// planes, exponents, scalars and C.
+template <bool GROUPED>
 __global__ void __launch_bounds__(THREADS, 1)
-oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
+oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P,
+           const GroupArgs G) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = (uint64_t*)(smem + (size_t)STAGES * STAGE_BYTES);
@@ -305,7 +388,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
-  const int total_tiles = P.tiles_m * P.tiles_n;
+  const int total_tiles = GROUPED ? G.n_items : P.tiles_m * P.tiles_n;
   const int group = P.group_m > 0 ? P.group_m : 1;
   constexpr int B_BOX = OZ_BLOCK;  // a box stays inside one 128-line block of the blocked layout
 
@@ -340,20 +423,21 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       unsigned long long issued = 0, seen = 0;  // k-blocks issued in this launch; last pace count read
       const unsigned long long chunk_mask = (unsigned long long)P.pace_chunk - 1;
       for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
-        int tm, tn;
-        tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
+        const Job J = job_of<GROUPED>(ct, P, G, group);
+        const int tm = J.tm;
         // f runs P.pf k-blocks ahead of q: its boxes are prefetched into L2 so that the
         // loads, issued when a stage frees up, find them there instead of in DRAM
-        const int64_t b0 = (int64_t)tn * BN;
+        const int64_t b0 = (int64_t)J.tn * BN;
+        auto ay = [&](int p_, int kb_) { return (int)(J.a_row0 + box_y(p_, (int64_t)tm * BM, kb_, J.a_rows_pad, J.nkb)); };
+        auto by_ = [&](int q_, int64_t line, int kb_) { return (int)(J.b_row0 + box_y(q_, line, kb_, J.b_rows_pad, J.nkb)); };
         auto prefetch = [&](const Seq& f) {
-          tma_prefetch_2d(&tmA, 0, box_y(f.p, (int64_t)tm * BM, f.kb, P.a_rows_pad, P.nkb));
-          for (int j = 0; j < BN / B_BOX; ++j)
-            tma_prefetch_2d(&tmB, 0, box_y(f.g - f.p, b0 + j * B_BOX, f.kb, P.b_rows_pad, P.nkb));
+          tma_prefetch_2d(&tmA, 0, ay(f.p, f.kb));
+          for (int j = 0; j < BN / B_BOX; ++j) tma_prefetch_2d(&tmB, 0, by_(f.g - f.p, b0 + j * B_BOX, f.kb));
         };
         Seq q, f;
-        f.start(P.s, P.nkb);
+        f.start(P.s, J.nkb);
         for (int i = 0; i < P.pf && !f.done(); ++i, f.next()) prefetch(f);
-        for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+        for (q.start(P.s, J.nkb); !q.done() && ok; q.next()) {
           if (P.pf > 0 && !f.done()) {
             prefetch(f);
             f.next();
@@ -365,12 +449,10 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
           const uint32_t fb = full0 + 8 * stage;
           mbar_expect_tx(fb, STAGE_BYTES);  // A box + the B boxes
           uint8_t* sa = smem + (size_t)stage * STAGE_BYTES;
-          tma_load_2d(smem_u32(sa), &tmA, 0, box_y(q.p, (int64_t)tm * BM, q.kb, P.a_rows_pad, P.nkb), fb);
+          tma_load_2d(smem_u32(sa), &tmA, 0, ay(q.p, q.kb), fb);
 #pragma unroll
-          for (int j = 0; j < BN / B_BOX; ++j) {
-            const int by = box_y(q.g - q.p, b0 + j * B_BOX, q.kb, P.b_rows_pad, P.nkb);
-            tma_load_2d(smem_u32(sa + A_BYTES + j * B_BOX * KB), &tmB, 0, by, fb);
-          }
+          for (int j = 0; j < BN / B_BOX; ++j)
+            tma_load_2d(smem_u32(sa + A_BYTES + j * B_BOX * KB), &tmB, 0, by_(q.g - q.p, b0 + j * B_BOX, q.kb), fb);
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1;
@@ -400,8 +482,9 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       constexpr uint64_t STAGE_STEP = (uint64_t)(STAGE_BYTES >> 4);  // descriptor address field per stage
       const uint32_t sa0 = smem_u32(smem);
       const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + A_BYTES);
+      auto nkb_of = [&](int ct) { return GROUPED ? G.probs[G.items[ct].x].nkb : P.nkb; };
       MmaCursor cur;
-      cur.start(blockIdx.x, total_tiles, P.s, P.nkb);
+      cur.start(blockIdx.x, gridDim.x, total_tiles, P.s, nkb_of);
       int stage = 0, buf = 0;
       uint32_t phase = 0, tph = 0;  // tph bit b: phase of accumulator b's full barrier
       uint64_t ad = ad0, bd = bd0;
@@ -417,7 +500,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         mma_f8(d_tmem, ad + 2, bd + 2, 1u);
         mma_f8(d_tmem, ad + 4, bd + 4, 1u);
         // ---- next k-block, while two MMAs are still queued
-        cur.next(gridDim.x, total_tiles, P.s, P.nkb);
+        cur.next(gridDim.x, total_tiles, P.s, nkb_of);
         const bool nvalid = cur.valid;
         const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
         const int nstage = stage + 1 == STAGES ? 0 : stage + 1;
@@ -466,11 +549,12 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
     int buf = 0;
     bool ok = true;
     for (int ct = blockIdx.x; ct < total_tiles && ok; ct += gridDim.x) {
-      int tm, tn;
-      tile_coords(ct, P.tiles_m, P.tiles_n, group, &tm, &tn);
+      const Job J = job_of<GROUPED>(ct, P, G, group);
+      const Epi E = epi_job<GROUPED>(ct, P, G);
+      const int tm = J.tm, tn = J.tn;
       bool first_pass = true;
       Seq q;
-      for (q.start(P.s, P.nkb); !q.done() && ok; q.next()) {
+      for (q.start(P.s, J.nkb); !q.done() && ok; q.next()) {
         if (!q.pass_last()) continue;
         // one lane waits, the warp follows: the TMEM loads below are warp-collective
         int okw = 1;
@@ -481,7 +565,7 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         tc_fence_after();
         const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
         const uint32_t tempty = tempty0 + 8 * buf;
-        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), P, (int64_t)tm * BM + row, (int64_t)tn * BN,
+        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), E, (int64_t)tm * BM + row, (int64_t)tn * BN,
                    [&] {  // accumulator consumed: hand it back to the MMA warp
                      tc_fence_before();
                      __syncwarp();
@@ -618,8 +702,9 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       constexpr uint64_t STAGE_STEP = (uint64_t)(PAIR_STAGE_BYTES >> 4);
       const uint32_t sa0 = smem_u32(smem);
       const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + PAIR_A_BYTES);
+      auto nkb_of = [&](int) { return P.nkb; };
       MmaCursor cur;
-      cur.start(pair_id, total_tiles, P.s, P.nkb);
+      cur.start(pair_id, num_pairs, total_tiles, P.s, nkb_of);
       int stage = 0, buf = 0;
       uint32_t phase = 0, tph = 0;
       uint64_t ad = ad0, bd = bd0;
@@ -633,7 +718,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         mma_f8_pair(d_tmem, ad, bd, first ? 0u : 1u);
         mma_f8_pair(d_tmem, ad + 2, bd + 2, 1u);
         mma_f8_pair(d_tmem, ad + 4, bd + 4, 1u);
-        cur.next(num_pairs, total_tiles, P.s, P.nkb);
+        cur.next(num_pairs, total_tiles, P.s, nkb_of);
         const bool nvalid = cur.valid;
         const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
         const int nstage = stage + 1 == PAIR_STAGES ? 0 : stage + 1;
@@ -677,6 +762,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;  // TMEM lane = row of this CTA's half of the tile
     double* slot = P.work + (size_t)blockIdx.x * (size_t)(BM * BN);
+    const Epi E = epi_of(P);
     uint32_t tphase[2] = {0, 0};
     int buf = 0;
     bool ok = true;
@@ -697,7 +783,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         tc_fence_after();
         const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN);
         const uint32_t tempty = lead_tempty0 + 8 * buf;
-        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), P, (int64_t)tm * PAIR_M + rank * 128 + row,
+        drain_pass(tbase, slot, row, q.g, first_pass, q.tile_last(), E, (int64_t)tm * PAIR_M + rank * 128 + row,
                    (int64_t)tn * BN, [&] {
                      tc_fence_before();
                      __syncwarp();
@@ -768,7 +854,9 @@ const DeviceSetup* device_setup() {
     d.status = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     if (d.status != cudaSuccess) return;
     if (d.sms <= 0) d.sms = 1;
-    d.status = cudaFuncSetAttribute(oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    d.status = cudaFuncSetAttribute(oz_gemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (d.status != cudaSuccess) return;
+    d.status = cudaFuncSetAttribute(oz_gemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (d.status != cudaSuccess) return;
     d.status = cudaFuncSetAttribute(oz_gemm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAIR_SMEM_BYTES);
     if (d.status != cudaSuccess) return;
@@ -801,7 +889,7 @@ cudaError_t launch(const CUtensorMap& ma, const CUtensorMap& mb, const Params& P
   if (d->status != cudaSuccess) return d->status;
   const int64_t tiles = (int64_t)P.tiles_m * P.tiles_n;
   const int ctas = tiles < d->sms ? (int)tiles : d->sms;  // the workspace has one slot per SM
-  oz_gemm_tc<<<ctas, THREADS, SMEM_BYTES, s>>>(ma, mb, P);
+  oz_gemm_tc<false><<<ctas, THREADS, SMEM_BYTES, s>>>(ma, mb, P, GroupArgs{nullptr, nullptr, 0});
   return cudaGetLastError();
 }
 
@@ -847,6 +935,97 @@ size_t ozaki_tc_workspace_bytes_for(int64_t m, int64_t n) {
 }
 int64_t ozaki_tc_pass_blocks() { return tc::PASS_BLOCKS; }
 int ozaki_tc_k_block() { return tc::KB; }
+
+cudaError_t ozaki_tc_grouped_image(const std::vector<GroupedProduct>& prods, const void* arena, size_t arena_bytes,
+                                   std::vector<unsigned char>& out, int* n_items) {
+  std::vector<tc::GroupProblem> recs;
+  std::vector<int4> items;
+  std::vector<int64_t> cost;
+  for (size_t i = 0; i < prods.size(); ++i) {
+    const GroupedProduct& p = prods[i];
+    const OzakiSplit& A = p.A;
+    const OzakiSplit& B = p.B;
+    if (p.m <= 0 || p.n <= 0) continue;
+    if (A.enc != OZ_ENC_E4M3 || B.enc != OZ_ENC_E4M3 || A.k_pad != B.k_pad || A.slices != B.slices ||
+        A.slices != prods[0].A.slices || A.rows_pad % tc::BM || B.rows_pad % tc::BN || A.k_pad % tc::KB ||
+        !A.blocked || !B.blocked)
+      return cudaErrorInvalidValue;
+    const int64_t aoff = (const char*)A.digits - (const char*)arena, boff = (const char*)B.digits - (const char*)arena;
+    if (aoff < 0 || boff < 0 || aoff % tc::KB || boff % tc::KB) return cudaErrorInvalidValue;
+    // every box of the planes lies inside the arena that the launch's tensor map covers
+    if ((size_t)aoff + (size_t)A.slices * (size_t)A.rows_pad * (size_t)A.k_pad > arena_bytes ||
+        (size_t)boff + (size_t)B.slices * (size_t)B.rows_pad * (size_t)B.k_pad > arena_bytes)
+      return cudaErrorInvalidValue;
+    tc::GroupProblem r;
+    r.a_row0 = aoff / tc::KB;
+    r.b_row0 = boff / tc::KB;
+    r.a_rows_pad = A.rows_pad;
+    r.b_rows_pad = B.rows_pad;
+    r.ea = A.exps;
+    r.eb = B.exps;
+    r.C = p.C;
+    r.ldc = p.ldc;
+    r.m = p.m;
+    r.n = p.n;
+    r.alpha = p.alpha;
+    r.beta = p.beta;
+    r.nkb = (int)(A.k_pad / tc::KB);
+    r.first = p.first_k_tile ? 1 : 0;
+    const int idx = (int)recs.size();
+    recs.push_back(r);
+    const int tm_n = (int)((p.m + tc::BM - 1) / tc::BM), tn_n = (int)((p.n + tc::BN - 1) / tc::BN);
+    for (int tm = 0; tm < tm_n; ++tm)
+      for (int tn = 0; tn < tn_n; ++tn) {
+        items.push_back(make_int4(idx, tm, tn, 0));
+        cost.push_back((int64_t)r.nkb);
+      }
+  }
+  // largest tiles first: dealt round-robin to the CTAs, the longest sequences start first
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+  const size_t rec_bytes = (recs.size() * sizeof(tc::GroupProblem) + 255) / 256 * 256;
+  out.assign(rec_bytes + items.size() * sizeof(int4), 0);
+  if (!recs.empty()) memcpy(out.data(), recs.data(), recs.size() * sizeof(tc::GroupProblem));
+  int4* it = (int4*)(out.data() + rec_bytes);
+  for (size_t i = 0; i < order.size(); ++i) it[i] = items[order[i]];
+  *n_items = (int)items.size();
+  return cudaSuccess;
+}
+
+cudaError_t ozaki_gemm_tc_grouped(const void* arena, size_t arena_bytes, int slices, const void* dev_image, int n_probs,
+                                  int n_items, double* work, int* err, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  if (!arena || !dev_image || !work || !err || arena_bytes / tc::KB > (size_t)INT32_MAX) return cudaErrorInvalidValue;
+  const tc::DeviceSetup* d = tc::device_setup();
+  if (!d) return cudaErrorInvalidDevice;
+  if (d->status != cudaSuccess) return d->status;
+  auto fn = tc::encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  // one map over the arena: A and B planes of every problem, as a column of 128-byte rows
+  CUtensorMap map;
+  cuuint64_t dims[2] = {(cuuint64_t)tc::KB, (cuuint64_t)(arena_bytes / tc::KB)};
+  cuuint64_t strides[1] = {(cuuint64_t)tc::KB};
+  cuuint32_t box[2] = {(cuuint32_t)tc::KB, (cuuint32_t)OZ_BLOCK};
+  cuuint32_t estr[2] = {1, 1};
+  if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(arena), dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  tc::Params P{};
+  P.s = slices;
+  P.work = (double*)((char*)work + tc::WORK_HEADER);
+  P.pace = (unsigned long long*)work;
+  P.err = err;
+  P.group_m = tc::GROUP_M;
+  P.epi_hint = tc::EPI_WAIT_HINT_NS;
+  P.pace_chunk = 64;
+  const size_t rec_bytes = ((size_t)n_probs * sizeof(tc::GroupProblem) + 255) / 256 * 256;
+  tc::GroupArgs G{(const tc::GroupProblem*)dev_image, (const int4*)((const char*)dev_image + rec_bytes), n_items};
+  const int ctas = n_items < d->sms ? n_items : d->sms;  // the workspace has one slot per SM
+  tc::oz_gemm_tc<true><<<ctas, tc::THREADS, tc::SMEM_BYTES, s>>>(map, map, P, G);
+  return cudaGetLastError();
+}
 
 cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, int64_t n, double alpha, double beta,
                           bool first_k_tile, double* C, int64_t ldc, double* work, int* err, cudaStream_t s) {
