@@ -67,6 +67,12 @@ WORKLOADS = {
     "ozaki8192": dict(m=8192, n=8192, k=8192, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
                       path="ozaki", tiles=(8192, 8192, 8192), streams=2,
                       desc="Ozaki-emulated FP64 GEMM m=n=k=8192 NN, u*2^e, e in [-20,20] (profiling size)"),
+    # one engine launch with the headline's k tile and slice count on a sixteenth of its tiles: the
+    # size the slice-product kernel is profiled at (a few GB on the device)
+    "ozaki8192k16384": dict(m=8192, n=8192, k=16384, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
+                            path="ozaki", tiles=(8192, 8192, 16384), streams=2,
+                            desc="Ozaki-emulated FP64 GEMM m=n=8192, k=16384 NN, u*2^e, e in [-20,20], one k tile "
+                                 "(profiling size of the headline's engine launch)"),
     # the out-of-core update m = n = 65536, k = 131072 (NT, alpha = -1, beta = 1) with every dimension
     # halved, so that its host operands fit this host's 199 GB of RAM
     "ooc_ozaki": dict(m=32768, n=32768, k=65536, ta="N", tb="T", alpha=-1.0, beta=1.0, kind=3, param=10.0,

@@ -2,6 +2,7 @@
 //   dmma    mma.sync m16n8k4 f64 (native FP64 tile kernel)
 //   imma    mma.sync m16n8k32 s8 -> s32 (IMMA Ozaki engine)
 //   tcgen05 tcgen05.mma.cta_group::1.kind::f8f6f4, M128 N256 K32, e4m3 operands resident in shared
+//           (and kind::f16 with bf16 operands, M128 N256 K16, the FP32 engine's instruction)
 //           memory, issued back to back from one thread (tcgen05 Ozaki engine, pipe ceiling)
 // Every CTA runs a fixed number of iterations; the tcgen05 probe's one wait is bounded by %globaltimer.
 //
@@ -120,7 +121,23 @@ __global__ void __launch_bounds__(128, 1) tcgen05_loop(int kblocks, int mode, lo
         }
       }
     }
-    for (int kb = 0; mode != 1 && kb < kblocks; ++kb) {
+    if (mode == 3) {  // kind::f16, bf16 operands (the FP32 engine's instruction), back to back
+      constexpr uint32_t IDESC_BF16 =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+      for (int kb = 0; kb < kblocks; ++kb) {
+        const uint32_t d = tmem + (uint32_t)(((kb >> 9) & 1) * 256);
+        const uint32_t acc0 = (kb & 511) ? 1u : 0u;
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                     ::"r"(d), "l"(ad), "l"(bd), "r"(IDESC_BF16), "r"(acc0));
+        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 2), "l"(bd + 2), "r"(IDESC_BF16));
+        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 4), "l"(bd + 4), "r"(IDESC_BF16));
+        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 6), "l"(bd + 6), "r"(IDESC_BF16));
+        const bool wrap = (kb & 3) == 3;
+        ad = wrap ? ad0 : ad + (49152 >> 4);
+        bd = wrap ? bd0 : bd + (49152 >> 4);
+      }
+    }
+    for (int kb = 0; mode != 1 && mode != 3 && kb < kblocks; ++kb) {
       const uint32_t d = tmem + (uint32_t)(((kb >> 9) & 1) * 256);
       const uint32_t acc0 = (kb & 511) ? 1u : 0u;
       asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
@@ -197,7 +214,7 @@ int main() {
       if (rep) printf("{\"probe\": \"imma_m16n8k32_s8\", \"tops\": %.3f}\n", ops / time_ms(e0, e1) / 1e9);
     }
   }
-  for (int mode = 0; mode < 3; ++mode) {  // tcgen05 e4m3 pipe
+  for (int mode = 0; mode < 4; ++mode) {  // tcgen05 e4m3 pipe (modes 0-2), bf16 pipe (mode 3)
     const int kblocks = 20000;
     const int smem = 4 * 49152 + 1024;
     long long* cyc = nullptr;
@@ -220,13 +237,17 @@ int main() {
       double c = 0;
       for (int i = 0; i < n; ++i) c += (double)h[i];
       c /= n;
-      const double flop = (double)sms * kblocks * (2.0 * 128 * 256 * 128);
-      static const char* form[3] = {"back_to_back", "bookkeeping_after_4th_mma", "probe_between_3rd_and_4th"};
-      printf("{\"probe\": \"tcgen05_f8f6f4_m128n256k32\", \"issue_loop\": \"%s\", \"tflops\": %.1f, "
+      // a k-block is 128 bytes of K: 128 e4m3 or 64 bf16 elements
+      const double kel = mode == 3 ? 64.0 : 128.0;
+      const double flop = (double)sms * kblocks * (2.0 * 128 * 256 * kel);
+      static const char* form[4] = {"back_to_back", "bookkeeping_after_4th_mma", "probe_between_3rd_and_4th",
+                                    "back_to_back"};
+      printf("{\"probe\": \"%s\", \"issue_loop\": \"%s\", \"tflops\": %.1f, "
              "\"cycles_per_kblock\": %.1f, \"flop_per_clk_per_sm\": %.0f, \"tflops_at_max_clock\": %.1f, "
              "\"wait_error\": %d}\n",
-             form[mode], flop / time_ms(e0, e1) / 1e9, c / kblocks, 2.0 * 128 * 256 * 128 * kblocks / c,
-             2.0 * 128 * 256 * 128 * kblocks / c * sms * (clk_khz * 1e3) / 1e12, herr);
+             mode == 3 ? "tcgen05_f16_bf16_m128n256k16" : "tcgen05_f8f6f4_m128n256k32", form[mode],
+             flop / time_ms(e0, e1) / 1e9, c / kblocks, 2.0 * 128 * 256 * kel * kblocks / c,
+             2.0 * 128 * 256 * kel * kblocks / c * sms * (clk_khz * 1e3) / 1e12, herr);
     }
     CK(cudaFree(cyc));
     CK(cudaFree(err));
