@@ -1434,6 +1434,7 @@ void drop_batch_graph(tmm_context* ctx) {
 // from the batch stream and join it.  The IMMA engine runs the same pipeline with one launch
 // per problem and k tile.
 constexpr int BATCH_OZ_CHUNKS = 4;
+constexpr int BATCH_OZ_SPLIT_STREAMS = 4;
 
 struct BatchOzRound {  // one grouped launch: the chunk's problems that have a k tile r
   int chunk, round, n_probs, n_items;
@@ -1565,12 +1566,15 @@ int plan_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev
   if (st) return st;
   if (ctx->oz_work.ptr != wbefore) *moved = true;
   if (!ctx->oz_fork) TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->oz_fork, cudaEventDisableTiming));
-  while (ctx->oz_branches.size() < 3) {  // copies in, splits and products, copies out
+  // products, copies in, copies out, the split streams
+  while (ctx->oz_branches.size() < 3 + (size_t)BATCH_OZ_SPLIT_STREAMS) {
     cudaStream_t bs;
     TMM_CUDA(ctx, cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
     ctx->oz_branches.push_back(bs);
   }
-  while (ctx->oz_branch_done.size() < 2 * (size_t)BATCH_OZ_CHUNKS + 2) {
+  // per chunk: copies landed, products done; the joins; the split fork and joins; the copies
+  // of the batch's other problems
+  while (ctx->oz_branch_done.size() < 2 * (size_t)BATCH_OZ_CHUNKS + 4 + (size_t)BATCH_OZ_SPLIT_STREAMS) {
     cudaEvent_t ev;
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     ctx->oz_branch_done.push_back(ev);
@@ -1580,21 +1584,31 @@ int plan_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev
 }
 
 // operands of problem d from the caller's host buffers into the arena, and C back
+// A column-major block of `cols` columns of `width` bytes between pitches dpitch and spitch:
+// one plain copy when both sides are contiguous (the copy engines move a 2D copy row by row,
+// and batch problems with short columns -- 64 rows of a float are 256 bytes -- crawl that
+// way), else a 2D copy.
+cudaError_t copy_block(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                       cudaMemcpyKind kind, cudaStream_t s) {
+  if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * cols, kind, s);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, s);
+}
+
 int copy_problem_in(tmm_context* ctx, const tmm_batch_problem& h, const tmm::BatchProblem& d, cudaStream_t s) {
   const size_t es = h.dtype == TMM_DOUBLE ? 8 : 4;
   if (d.m == 0 || d.n == 0) return TMM_SUCCESS;
   if (d.k > 0) {
     const int64_t ar = d.opa == tmm::OP_N ? d.m : d.k, ac = d.opa == tmm::OP_N ? d.k : d.m;
     const int64_t br = d.opb == tmm::OP_N ? d.k : d.n, bc = d.opb == tmm::OP_N ? d.n : d.k;
-    TMM_CUDA(ctx, cudaMemcpy2DAsync((void*)d.a, (size_t)ar * es, h.a, (size_t)h.ld_a * es, (size_t)ar * es, (size_t)ac,
-                                    cudaMemcpyHostToDevice, s));
-    TMM_CUDA(ctx, cudaMemcpy2DAsync((void*)d.b, (size_t)br * es, h.b, (size_t)h.ld_b * es, (size_t)br * es, (size_t)bc,
-                                    cudaMemcpyHostToDevice, s));
+    TMM_CUDA(ctx, copy_block((void*)d.a, (size_t)ar * es, h.a, (size_t)h.ld_a * es, (size_t)ar * es, (size_t)ac,
+                             cudaMemcpyHostToDevice, s));
+    TMM_CUDA(ctx, copy_block((void*)d.b, (size_t)br * es, h.b, (size_t)h.ld_b * es, (size_t)br * es, (size_t)bc,
+                             cudaMemcpyHostToDevice, s));
     ctx->stats.h2d_bytes += (uint64_t)(ar * ac + br * bc) * es;
   }
   if (h.beta != 0.0) {
-    TMM_CUDA(ctx, cudaMemcpy2DAsync(d.c, (size_t)d.m * es, h.c, (size_t)h.ld_c * es, (size_t)d.m * es, (size_t)d.n,
-                                    cudaMemcpyHostToDevice, s));
+    TMM_CUDA(ctx, copy_block(d.c, (size_t)d.m * es, h.c, (size_t)h.ld_c * es, (size_t)d.m * es, (size_t)d.n,
+                             cudaMemcpyHostToDevice, s));
     ctx->stats.h2d_bytes += (uint64_t)(d.m * d.n) * es;
   }
   return TMM_SUCCESS;
@@ -1603,8 +1617,8 @@ int copy_problem_in(tmm_context* ctx, const tmm_batch_problem& h, const tmm::Bat
 int copy_problem_out(tmm_context* ctx, const tmm_batch_problem& h, const tmm::BatchProblem& d, cudaStream_t s) {
   const size_t es = h.dtype == TMM_DOUBLE ? 8 : 4;
   if (d.m == 0 || d.n == 0) return TMM_SUCCESS;
-  TMM_CUDA(ctx, cudaMemcpy2DAsync(h.c, (size_t)h.ld_c * es, d.c, (size_t)d.m * es, (size_t)d.m * es, (size_t)d.n,
-                                  cudaMemcpyDeviceToHost, s));
+  TMM_CUDA(ctx, copy_block(h.c, (size_t)h.ld_c * es, d.c, (size_t)d.m * es, (size_t)d.m * es, (size_t)d.n,
+                           cudaMemcpyDeviceToHost, s));
   ctx->stats.d2h_bytes += (uint64_t)(d.m * d.n) * es;
   return TMM_SUCCESS;
 }
@@ -1619,6 +1633,8 @@ int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& 
   const size_t nch = plan.chunks.size();
   cudaEvent_t* ev_in = &ctx->oz_branch_done[0];
   cudaEvent_t* ev_done = &ctx->oz_branch_done[(size_t)BATCH_OZ_CHUNKS];
+  cudaEvent_t ev_split_fork = ctx->oz_branch_done[2 * (size_t)BATCH_OZ_CHUNKS + 2];
+  cudaEvent_t* ev_split_done = &ctx->oz_branch_done[2 * (size_t)BATCH_OZ_CHUNKS + 3];
   TMM_CUDA(ctx, cudaEventRecord(ctx->oz_fork, s));
   TMM_CUDA(ctx, cudaStreamWaitEvent(comp, ctx->oz_fork, 0));
   if (host) {
@@ -1641,6 +1657,11 @@ int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& 
       const BatchOzRound& L = plan.launches[li];
       std::vector<std::pair<tmm::OzakiSplit, tmm::OzakiSplit>> views;
       std::vector<int> pos;
+      // the splits of small problems are latency-bound kernels: they run on BATCH_OZ_SPLIT_STREAMS
+      // streams forked from the compute stream and joined before the grouped launch
+      TMM_CUDA(ctx, cudaEventRecord(ev_split_fork, comp));
+      for (int q = 0; q < BATCH_OZ_SPLIT_STREAMS; ++q)
+        TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->oz_branches[3 + (size_t)q], ev_split_fork, 0));
       for (int j : plan.chunks[c]) {
         const tmm::BatchProblem& d = dev[(size_t)plan.ids[(size_t)j]];
         const int64_t k0 = (int64_t)L.round * plan.tk[(size_t)j];
@@ -1649,12 +1670,17 @@ int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& 
         batch_oz_views(ctx, plan, d, (size_t)j, L.round, &va, &vb);
         const double* ab = d.opa == tmm::OP_N ? (const double*)d.a + k0 * d.lda : (const double*)d.a + k0;
         const double* bb = d.opb == tmm::OP_N ? (const double*)d.b + k0 : (const double*)d.b + k0 * d.ldb;
-        cudaError_t e = tmm::ozaki_split(ab, d.lda, d.opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, d.m, va.kk, va, comp);
+        cudaStream_t ss = ctx->oz_branches[3 + pos.size() % BATCH_OZ_SPLIT_STREAMS];
+        cudaError_t e = tmm::ozaki_split(ab, d.lda, d.opa == tmm::OP_N ? tmm::OP_N : tmm::OP_T, d.m, va.kk, va, ss);
         if (e == cudaSuccess)
-          e = tmm::ozaki_split(bb, d.ldb, d.opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, d.n, vb.kk, vb, comp);
+          e = tmm::ozaki_split(bb, d.ldb, d.opb == tmm::OP_N ? tmm::OP_T : tmm::OP_N, d.n, vb.kk, vb, ss);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "batched ozaki split");
         views.emplace_back(va, vb);
         pos.push_back(j);
+      }
+      for (int q = 0; q < BATCH_OZ_SPLIT_STREAMS; ++q) {
+        TMM_CUDA(ctx, cudaEventRecord(ev_split_done[q], ctx->oz_branches[3 + (size_t)q]));
+        TMM_CUDA(ctx, cudaStreamWaitEvent(comp, ev_split_done[q], 0));
       }
       cudaError_t e = cudaSuccess;
       if (ctx->oz_engine == tmm::OZ_ENGINE_TCGEN05) {
@@ -1788,11 +1814,19 @@ int enqueue_batch(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, c
   const void* dwork = (const char*)ctx->batch_meta.ptr + (rec * (size_t)count + 255) / 256 * 256;
   std::vector<char> on_branch((size_t)count, 0);
   for (int id : oz.ids) on_branch[(size_t)id] = 1;
-  // the Ozaki branches first: they move their own operands
+  // the Ozaki pipeline first: it moves its own operands; the other problems' operands follow
+  // its chunks on the same copy stream, so that the engine's chunks are not kept waiting
   int st = enqueue_batch_ozaki(ctx, dev, oz, s, host);
   if (st) return st;
+  const bool after_oz = !oz.ids.empty();
+  cudaStream_t cs = after_oz ? ctx->oz_branches[1] : s;
   for (int i = 0; i < count; ++i)
-    if (!on_branch[(size_t)i] && (st = copy_problem_in(ctx, host[i], dev[i], s))) return st;
+    if (!on_branch[(size_t)i] && (st = copy_problem_in(ctx, host[i], dev[i], cs))) return st;
+  if (after_oz) {
+    cudaEvent_t ev = ctx->oz_branch_done[2 * (size_t)BATCH_OZ_CHUNKS + 3 + (size_t)BATCH_OZ_SPLIT_STREAMS];
+    TMM_CUDA(ctx, cudaEventRecord(ev, cs));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(s, ev, 0));
+  }
   if ((st = fork_batch_f32(ctx, dev, f32, s, false))) return st;
   cudaError_t e = tmm::batch_launch(dprobs, count, dwork, n_f64, n_work - n_f64, any_k0, s, ctx->batch_aux,
                                     ctx->batch_fork, ctx->batch_join);
