@@ -109,6 +109,14 @@ int tmm_gemm_device(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int
                     const void* alpha, const void* a_dev, int64_t ld_a, const void* b_dev, int64_t ld_b,
                     const void* beta, void* c_dev, int64_t ld_c, void* stream);
 
+/* No counterpart in the reference (its calls are synchronous and report every failure).
+ * Device-side status of the asynchronous work this context has enqueued through
+ * tmm_gemm_device: waits for `stream` (a cudaStream_t; NULL: legacy default stream), then
+ * returns TMM_ERROR_TIMEOUT if a tensor-core kernel of this context gave up a pipeline wait
+ * (after about a second; its C is then incomplete) since the last check, TMM_SUCCESS
+ * otherwise, and clears what it read.  The synchronous calls check this themselves. */
+int tmm_device_status(tmm_context* ctx, void* stream);
+
 /* No counterpart in the reference.  The Ozaki (emulated FP64) product on
  * device operands for callers that cannot allocate device memory while they
  * run -- a framework whose caching allocator already owns the GPU, or a

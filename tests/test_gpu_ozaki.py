@@ -152,6 +152,29 @@ def test_device_entry_matches_host_entry(tmm, engine):
     np.testing.assert_array_equal(dc.cpu().numpy(), host)
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_device_status_after_asynchronous_calls(tmm, dtype):
+    """tmm_device_status waits for the stream and reports no gave-up wait after ordinary
+    device-resident calls on the tensor-core engines (FP64 on the Ozaki engine, FP32 on the
+    FP32 engine); the results are the host entry's."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(13)
+    m, n, k = 384, 320, 512
+    a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k, dtype=dtype)
+    ctx = tmm.make_context(dtype, 2, 4096, 4096, 4096)
+    if dtype == np.float64:
+        ctx.set_path(tmm.PATH_OZAKI, 11)
+        ctx.set_ozaki_engine("tcgen05")
+    host = c.copy()
+    tmm.gemm(ctx, "N", "T", m, n, k, 1.0, a, lda, b, ldb, 0.0, host, ldc)
+    da, db, dc = (torch.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        tmm.gemm_device(ctx, "N", "T", m, n, k, 1.0, da, lda, db, ldb, 0.0, dc, ldc, stream=s.cuda_stream)
+    assert ctx.device_status(s.cuda_stream) == 0
+    np.testing.assert_array_equal(dc.cpu().numpy(), host)
+
+
 @pytest.mark.parametrize("engine", ENGINES)
 def test_out_of_core_ozaki_matches_in_core(tmm, engine):
     rng = np.random.default_rng(13)

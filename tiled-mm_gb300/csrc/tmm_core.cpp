@@ -1093,6 +1093,15 @@ static int gemm_resident(tmm_context* ctx, char trans_a, char trans_b, int64_t m
   return st;
 }
 
+extern "C" int tmm_device_status(tmm_context* ctx, void* stream) {
+  if (!ctx) return fail(nullptr, TMM_ERROR_INVALID_ARGUMENT, "tmm_device_status: null context");
+  DeviceGuard dg(ctx->device);
+  TMM_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+  int st = check_oz_error(ctx);
+  if (!st) st = check_f32_error(ctx);
+  return st;
+}
+
 extern "C" int tmm_gemm(tmm_context* ctx, char trans_a, char trans_b, int64_t m, int64_t n, int64_t k,
                         const void* alpha, const void* a, int64_t ld_a, const void* b, int64_t ld_b,
                         const void* beta, void* c, int64_t ld_c, int pin_host_buffers, int copy_c_back) {

@@ -59,6 +59,7 @@ SIGNATURES = {
                                             C.c_double, _p, _i64, _ci, _i64, _p]),
     "tmm_ozaki_noalloc_status": (_ci, [_p]),
     "tmm_gemm_batched": (_ci, [_p, _ci, _p, _ci]),
+    "tmm_device_status": (_ci, [_p, _p]),
     "tmm_xt_create": (_ci, [C.POINTER(_p)]),
     "tmm_xt_destroy": (_ci, [_p]),
     "tmm_xt_set_block_dim": (_ci, [_p, _ci]),
@@ -302,6 +303,11 @@ class MMHandle:
         busy, span = C.c_double(), C.c_double()
         _check(_lib.tmm_get_kernel_busy_time(self._h, C.byref(busy), C.byref(span)), self._h)
         return busy.value, span.value
+
+    def device_status(self, stream: int | None = None) -> int:
+        """Waits for `stream`; TMM_ERROR_TIMEOUT (6) if a kernel of this context gave up a pipeline
+        wait since the last check, else 0."""
+        return _lib.tmm_device_status(self._h, stream)
 
     def stats(self) -> dict:
         s = Stats()
