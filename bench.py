@@ -108,6 +108,16 @@ WORKLOADS = {
                              desc="512 GEMMs, m,n,k log-uniform [64,4096], half FP64 half FP32, random trans, "
                                   "uniform[-1,1), pinned host buffers, captured CUDA graph; FP64 problems on the Ozaki "
                                   "path at the slice count that meets the native batch's error metric"),
+    # the out-of-core update m = n = k = 100000 (TN, ld padded by 64, alpha = 1, beta = 0.5, tiles
+    # 8192^3, 3 streams) at a quarter of each dimension (a host-link-to-DMMA ratio the full size
+    # shares; a full-size call takes about 30 minutes on the DMMA pipe), with the device memory capped
+    # at 6 GiB -- the footprint of 3 streams x 3 tiles of 512 MiB -- so that A and B tiles are evicted
+    # and sent again as the C tiles advance
+    "ooc_native": dict(m=25000, n=25000, k=25000, ta="T", tb="N", alpha=1.0, beta=0.5, kind=0, param=0.0,
+                       path="native", tiles=(8192, 8192, 8192), streams=3, ld_pad=64, mem_limit=6 << 30,
+                       desc="Out-of-core native FP64 GEMM m=n=k=25000 TN, ld padded by 64, alpha=1, beta=0.5, "
+                            "uniform[-1,1), tiles 8192^3, 3 streams, pinned host buffers, device memory capped at "
+                            "6 GiB so that tiles are evicted and streamed"),
     "native4096": dict(m=4096, n=4096, k=4096, ta="N", tb="N", alpha=1.0, beta=1.0, kind=0, param=0.0,
                        path="native", tiles=(2048, 2048, 2048), streams=2,
                        desc="FP64 GEMM m=n=k=4096 NN, uniform[-1,1), alpha=beta=1, tiles 2048, 2 streams"),
@@ -386,10 +396,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
 
     dev = torch.device("cuda")
     m, n, k = w["m"], w["n"], w["k"]
-    lda = m if w["ta"] == "N" else k
-    ldb = k if w["tb"] == "N" else n
     a_rows, a_cols = (m, k) if w["ta"] == "N" else (k, m)
     b_rows, b_cols = (k, n) if w["tb"] == "N" else (n, k)
+    pad = w.get("ld_pad", 0)  # leading dimensions padded beyond the stored rows
+    lda, ldb, ldc = a_rows + pad, b_rows + pad, m + pad
     flops = 2.0 * m * n * k
     stream = torch.cuda.current_stream()
     sid = stream.cuda_stream
@@ -406,13 +416,13 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         log(f"slices = {slices}")
 
     # ---- device-resident operands
-    A = torch.empty(a_rows * a_cols, dtype=torch.float64, device=dev)
-    B = torch.empty(b_rows * b_cols, dtype=torch.float64, device=dev)
-    Cd = torch.empty(m * n, dtype=torch.float64, device=dev)
+    A = torch.zeros(lda * a_cols, dtype=torch.float64, device=dev)
+    B = torch.zeros(ldb * b_cols, dtype=torch.float64, device=dev)
+    Cd = torch.zeros(ldc * n, dtype=torch.float64, device=dev)
     # (the row-factor kinds scale the rows of the stored A and of the stored B)
-    tmm.fill_device(A.data_ptr(), a_rows, a_cols, a_rows, w["kind"], w["param"], seed=rank, mat_id=0, stream=sid)
-    tmm.fill_device(B.data_ptr(), b_rows, b_cols, b_rows, w["kind"], w["param"], seed=rank, mat_id=1, stream=sid)
-    tmm.fill_device(Cd.data_ptr(), m, n, m, w.get("kind_c", w["kind"]), w["param"], seed=rank, mat_id=2, stream=sid)
+    tmm.fill_device(A.data_ptr(), a_rows, a_cols, lda, w["kind"], w["param"], seed=rank, mat_id=0, stream=sid)
+    tmm.fill_device(B.data_ptr(), b_rows, b_cols, ldb, w["kind"], w["param"], seed=rank, mat_id=1, stream=sid)
+    tmm.fill_device(Cd.data_ptr(), m, n, ldc, w.get("kind_c", w["kind"]), w["param"], seed=rank, mat_id=2, stream=sid)
     C0 = Cd.clone()
     ctx = tmm.make_context(np.float64, w["streams"], *w["tiles"])
     if slices:
@@ -422,7 +432,7 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
     def dev_step():
-        tmm.gemm_device(ctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, m, stream=sid)
+        tmm.gemm_device(ctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, ldc, stream=sid)
 
     for _ in range(args.warmup):
         Cd.copy_(C0)
@@ -465,14 +475,14 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     a_h, b_h = A.cpu().numpy(), B.cpu().numpy()
     c_out = Cd.cpu().numpy()
     c0_h = C0.cpu().numpy() if w["beta"] != 0 else None
-    e_ours = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m, c_out, m,
-                              n_samples=args.samples, seed=11)
+    e_ours = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, ldc, c_out,
+                              ldc, n_samples=args.samples, seed=11)
     result["error_metric"] = e_ours
 
     # ---- the error at each slice count on the full problem (one untimed-for-the-value call each,
     # event-timed for reference), beside the native path's error below
     if w["path"] == "ozaki" and args.sweep_slices:
-        c_pin = torch.empty(m * n, dtype=torch.float64).pin_memory()
+        c_pin = torch.empty(ldc * n, dtype=torch.float64).pin_memory()
         sweep = {}
         for s_try in [int(x) for x in args.sweep_slices.split(",")]:
             ctx.set_path(tmm.PATH_OZAKI, s_try)
@@ -483,8 +493,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             ev[1].synchronize()
             t_s = ev[0].elapsed_time(ev[1]) / 1e3
             c_pin.copy_(Cd)
-            e_s = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m,
-                                   c_pin.numpy(), m, n_samples=args.samples, seed=11)
+            e_s = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, ldc,
+                                   c_pin.numpy(), ldc, n_samples=args.samples, seed=11)
             sweep[s_try] = {"error_metric": e_s, "tflops": flops / t_s / 1e12, "slice_pairs": s_try * (s_try + 1) // 2}
             log(f"full-size sweep: slices={s_try} metric={e_s:.3e} {flops / t_s / 1e12:.1f} TFLOP/s")
         ctx.set_path(tmm.PATH_OZAKI, slices)
@@ -496,13 +506,13 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
         nctx = tmm.make_context(np.float64, 1, *w["tiles"])
         Cd.copy_(C0)
         ev[0].record(stream)
-        tmm.gemm_device(nctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, m, stream=sid)
+        tmm.gemm_device(nctx, w["ta"], w["tb"], m, n, k, w["alpha"], A, lda, B, ldb, w["beta"], Cd, ldc, stream=sid)
         ev[1].record(stream)
         ev[1].synchronize()
         t_nat = ev[0].elapsed_time(ev[1]) / 1e3
         c_nat = Cd.cpu().numpy()
-        e_nat = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, m, c_nat,
-                                 m, n_samples=args.samples, seed=11)
+        e_nat = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], a_h, lda, b_h, ldb, w["beta"], c0_h, ldc, c_nat,
+                                 ldc, n_samples=args.samples, seed=11)
         result["native"] = {"tflops": flops / t_nat / 1e12, "seconds": t_nat, "error_metric": e_nat,
                             "kernel": "DMMA mma.sync m16n8k4 f64"}
         nctx.close()
@@ -512,12 +522,12 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     # ---- end to end through the public host-pointer call
     pageable = w.get("pageable", False)
     if pageable:  # ordinary (pageable) host memory; registered by the call itself when w["pin"]
-        ha, hb, hc = a_h, b_h, c0_h.copy() if c0_h is not None else np.zeros(m * n)
+        ha, hb, hc = a_h, b_h, c0_h.copy() if c0_h is not None else np.zeros(ldc * n)
         keep = []
     else:
-        pa = tmm.PinnedArray((a_rows * a_cols,))
-        pb = tmm.PinnedArray((b_rows * b_cols,))
-        pc = tmm.PinnedArray((m * n,))
+        pa = tmm.PinnedArray((lda * a_cols,))
+        pb = tmm.PinnedArray((ldb * b_cols,))
+        pc = tmm.PinnedArray((ldc * n,))
         pa.array[:] = a_h
         pb.array[:] = b_h
         ha, hb, hc = pa.array, pb.array, pc.array
@@ -530,6 +540,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     autotune = w.get("policy") == "autotune" and not args.tiles
     if autotune:
         hctx.set_tile_policy(tmm.TILE_POLICY_AUTOTUNE)
+    if w.get("mem_limit"):  # a device-memory cap that makes the tiles stream (evicted and sent again)
+        hctx.set_memory_limit(w["mem_limit"])
     if slices:
         hctx.set_path(tmm.PATH_OZAKI, slices)
         hctx.set_ozaki_engine(w["engine"])
@@ -537,7 +549,7 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
     e2e_times = []
 
     def e2e_call():
-        tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], hc, m,
+        tmm.gemm(hctx, w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], hc, ldc,
                  pin_host_buffers=w.get("pin", False), copy_c_back=copy_back)
 
     # warm-up; with the autotuner, until it has timed its candidates (each warm-up call runs one)
@@ -557,6 +569,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             e2e_times.append(time.perf_counter() - t0)
     e2e_kernel_s, _ = hctx.kernel_time()
     e2e_busy_s, e2e_span_s = hctx.kernel_busy_time()
+    e2e_error = None
+    if copy_back:  # the last call's C, sampled against compensated dot products on the host
+        e2e_error = tmm.error_metric(w["ta"], w["tb"], m, n, k, w["alpha"], ha, lda, hb, ldb, w["beta"], c_init, ldc,
+                                     hc, ldc, n_samples=min(args.samples, 256), seed=11)
     hctx.set_kernel_timing(False)
     st = hctx.stats()
     t_e2e = max_over_ranks(dist, float(np.mean(e2e_times)))
@@ -573,6 +589,10 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
                      "engine_busy_seconds_per_step": e2e_busy_s / max(1, args.e2e_steps),
                      "engine_launch_seconds_sum_per_step": e2e_kernel_s / max(1, args.e2e_steps),
                      "clocks": e2e_clk.summary()}
+    if e2e_error is not None:
+        result["e2e"]["error_metric"] = e2e_error
+    if w.get("mem_limit"):
+        result["e2e"]["device_memory_limit_bytes"] = w["mem_limit"]
     result["e2e"]["direct_bytes_per_step"] = st["direct_bytes"]
     result["tiles"] = [st["tile_m"], st["tile_n"], st["tile_k"], st["n_streams"]]
     if autotune:
@@ -656,6 +676,17 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
                               "frac": achieved / peak, "traffic": None, "kernel": "gemm_f64_dmma",
                               "peak_source": "mma.sync m16n8k4 f64 issue rate measured on this GPU (engine_rates "
                                              "probe)"}
+        # the host-pointer call's bound: the slower of the products at the DMMA issue rate and the
+        # host-link traffic it moved (tiles sent again after eviction included) at the measured bandwidth
+        link = host_link_bandwidth(torch)
+        t_compute = flops / (peak * 1e12)
+        t_h2d = result["e2e"]["h2d_bytes_per_step"] / (link["h2d_gbs"] * 1e9)
+        t_d2h = result["e2e"]["d2h_bytes_per_step"] / (link["d2h_gbs"] * 1e9)
+        t_roof = max(t_compute, t_h2d, t_d2h)
+        result["e2e"]["roofline"] = {"t_roof_seconds": t_roof, "t_measured_seconds": result["e2e"]["seconds_per_step"],
+                                     "frac": t_roof / result["e2e"]["seconds_per_step"],
+                                     "terms_seconds": {"compute": t_compute, "h2d": t_h2d, "d2h": t_d2h},
+                                     "link_gbs": link}
     return result
 
 

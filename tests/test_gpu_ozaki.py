@@ -66,13 +66,15 @@ def test_bit_exact_vs_oracle(tmm, oracle, engine, trans, shape, tiles):
     np.testing.assert_array_equal(out, want)
 
 
-@pytest.mark.parametrize("cluster", ["1", "pair"])
+@pytest.mark.parametrize("cluster", ["1", "pair", "pair7"])
 @pytest.mark.parametrize("shape", [(700, 530, 1100), (1100, 300, 700), (129, 600, 257)])
 def test_tcgen05_engine_forms_bit_exact(tmm, oracle, monkeypatch, cluster, shape):
     """Both engine forms -- one CTA per SM on 128 x 256 tiles, and CTA pairs issuing
     cta_group::2 MMAs on 256 x 256 tiles (a peer CTA whose rows are all padding at
-    m = 129) -- give the oracle's bits."""
-    monkeypatch.setenv("TMM_TC_CLUSTER", cluster)
+    m = 129), the latter with its 6- and 7-stage rings -- give the oracle's bits."""
+    monkeypatch.setenv("TMM_TC_CLUSTER", cluster[:4])
+    if cluster == "pair7":
+        monkeypatch.setenv("TMM_TC_PAIR_STAGES", "7")
     m, n, k = shape
     rng = np.random.default_rng(m * 7 + n)
     a, lda, b, ldb, c, ldc = make_problem(rng, "N", "T", m, n, k, pad=1, kind="uexp")

@@ -599,22 +599,24 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
 // arrivals).  Each CTA drains its own 128 TMEM lanes = its 128 tile rows, with the
 // pass sequence, FP64 recombination and fused epilogue of oz_gemm_tc.
 constexpr int PAIR_M = 256;
-constexpr int PAIR_STAGES = 6;
+constexpr int PAIR_STAGES = 6;  // the default ring; a 7-stage instance fills 227 KB (TMM_TC_PAIR_STAGES=7)
 constexpr int PAIR_A_BYTES = 128 * KB, PAIR_B_BYTES = 128 * KB, PAIR_STAGE_BYTES = PAIR_A_BYTES + PAIR_B_BYTES;
-constexpr size_t PAIR_SMEM_BYTES = (size_t)PAIR_STAGES * PAIR_STAGE_BYTES + 1024 + 256;
+constexpr size_t pair_smem_bytes(int stages) { return (size_t)stages * PAIR_STAGE_BYTES + 1024 + 256; }
+static_assert(pair_smem_bytes(7) <= 232448, "7 pair stages exceed the 227 KB of shared memory per CTA");
 
+template <int NST>
 __global__ void __launch_bounds__(THREADS, 1)
 oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const Params P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* bars = (uint64_t*)(smem + (size_t)PAIR_STAGES * PAIR_STAGE_BYTES);
-  // bars: full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2]
-  volatile int* abort_flag = (volatile int*)(bars + 2 * PAIR_STAGES + 4);
-  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * PAIR_STAGES + 5);
+  uint64_t* bars = (uint64_t*)(smem + (size_t)NST * PAIR_STAGE_BYTES);
+  // bars: full[NST], empty[NST], tfull[2], tempty[2]
+  volatile int* abort_flag = (volatile int*)(bars + 2 * NST + 4);
+  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * NST + 5);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_ctarank();  // 0: leader
-  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + PAIR_STAGES);
-  const uint32_t tfull0 = smem_u32(bars + 2 * PAIR_STAGES), tempty0 = smem_u32(bars + 2 * PAIR_STAGES + 2);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NST);
+  const uint32_t tfull0 = smem_u32(bars + 2 * NST), tempty0 = smem_u32(bars + 2 * NST + 2);
   const uint32_t lead_full0 = mapa(full0, 0), lead_tempty0 = mapa(tempty0, 0);
   const uint32_t peer_abort = mapa(smem_u32((const void*)abort_flag), rank ^ 1u);
   const int pair_id = blockIdx.x >> 1, num_pairs = gridDim.x >> 1;
@@ -623,7 +625,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   constexpr uint16_t BOTH = 3;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < PAIR_STAGES; ++i) {
+    for (int i = 0; i < NST; ++i) {
       mbar_init(full0 + 8 * i, 1);   // the leader's expect_tx arrival (+ both CTAs' bytes)
       mbar_init(empty0 + 8 * i, 1);  // one multicast commit
     }
@@ -679,7 +681,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
           const uint32_t fb = lead_full0 + 8 * stage;
           tma_load_2d_pair(smem_u32(sa), &tmA, 0, box_y(q.p, arow, q.kb, P.a_rows_pad, P.nkb), fb);
           tma_load_2d_pair(smem_u32(sa + PAIR_A_BYTES), &tmB, 0, box_y(q.g - q.p, brow, q.kb, P.b_rows_pad, P.nkb), fb);
-          if (++stage == PAIR_STAGES) {
+          if (++stage == NST) {
             stage = 0;
             phase ^= 1;
           }
@@ -687,9 +689,9 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       }
       if (P.pace_lag) red_add_u64(P.pace, PACE_DONE);
       // drain: every copy issued has been consumed before the CTA may exit (bounded)
-      for (int i = 0; i < PAIR_STAGES; ++i) {
+      for (int i = 0; i < NST; ++i) {
         (void)mbar_wait_pair<false>(empty0 + 8 * stage, phase ^ 1, abort_flag, peer_abort, P.err, false);
-        if (++stage == PAIR_STAGES) {
+        if (++stage == NST) {
           stage = 0;
           phase ^= 1;
         }
@@ -721,7 +723,7 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         cur.next(num_pairs, total_tiles, P.s, nkb_of);
         const bool nvalid = cur.valid;
         const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
-        const int nstage = stage + 1 == PAIR_STAGES ? 0 : stage + 1;
+        const int nstage = stage + 1 == NST ? 0 : stage + 1;
         const uint32_t nphase = nstage == 0 ? phase ^ 1u : phase;
         const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
         const bool ready = nvalid && !nfirst && mbar_try_wait(full0 + 8 * nstage, nphase);
@@ -858,7 +860,11 @@ const DeviceSetup* device_setup() {
     if (d.status != cudaSuccess) return;
     d.status = cudaFuncSetAttribute(oz_gemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
     if (d.status != cudaSuccess) return;
-    d.status = cudaFuncSetAttribute(oz_gemm_tc_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAIR_SMEM_BYTES);
+    d.status = cudaFuncSetAttribute(oz_gemm_tc_pair<PAIR_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pair_smem_bytes(PAIR_STAGES));
+    if (d.status != cudaSuccess) return;
+    d.status = cudaFuncSetAttribute(oz_gemm_tc_pair<7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)pair_smem_bytes(7));
     if (d.status != cudaSuccess) return;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
@@ -868,10 +874,10 @@ const DeviceSetup* device_setup() {
     at[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3((unsigned)((d.sms / 2) * 2));
     cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = PAIR_SMEM_BYTES;
+    cfg.dynamicSmemBytes = pair_smem_bytes(7);  // the larger instance: its count holds for both
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    d.status = cudaOccupancyMaxActiveClusters(&d.max_pairs, oz_gemm_tc_pair, &cfg);
+    d.status = cudaOccupancyMaxActiveClusters(&d.max_pairs, oz_gemm_tc_pair<7>, &cfg);
     if (d.status == cudaSuccess && d.max_pairs <= 0) d.status = cudaErrorInvalidConfiguration;
   });
   return &d;
@@ -909,11 +915,14 @@ cudaError_t launch_pair(const CUtensorMap& ma, const CUtensorMap& mb, const Para
   at[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3((unsigned)(pairs * 2));
   cfg.blockDim = dim3(THREADS);
-  cfg.dynamicSmemBytes = PAIR_SMEM_BYTES;
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, oz_gemm_tc_pair, ma, mb, P);
+  int stages = PAIR_STAGES;
+  if (const char* env = getenv("TMM_TC_PAIR_STAGES")) stages = atoi(env) == 7 ? 7 : PAIR_STAGES;
+  cfg.dynamicSmemBytes = pair_smem_bytes(stages);
+  if (stages == 7) return cudaLaunchKernelEx(&cfg, oz_gemm_tc_pair<7>, ma, mb, P);
+  return cudaLaunchKernelEx(&cfg, oz_gemm_tc_pair<PAIR_STAGES>, ma, mb, P);
 }
 
 }  // namespace tc
