@@ -48,7 +48,7 @@ def _newer(target: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     OUT.mkdir(parents=True, exist_ok=True)
-    headers = sorted(CSRC.glob("*.h")) + sorted((PKG.parent / "include").glob("*.h"))
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted((PKG.parent / "include").glob("*.h"))
     srcs = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
     objs = []
     jobs = []
