@@ -108,32 +108,45 @@ struct Seq {
   }
 };
 
-// Position of the MMA issuer in its (tile, sequence) order: tiles ct, ct + stride, ...
-// nkb_of(ct) gives tile ct's k-blocks; the next tile's count is read when a tile starts, so
+// The MMA issuer's walk of the same sequence.  It needs only where passes begin and end,
+// not (g, p, kb), so it counts k-blocks down: between two MMAs of the pipe's short queue
+// the issuing thread runs two decrements and a compare instead of the sequence's nested
+// counters (measured with the loads and drains switched off in a scratch build: 658-670
+// cycles per k-block of 4 MMAs with the nested counters, against 512 back to back).
+// Tiles ct, ct + stride, ...; nkb_of(ct) gives tile ct's k-blocks, read one tile ahead so
 // that a lookup in global memory (grouped launches) is not waited on at the tile change.
-struct MmaCursor {
-  Seq q;
-  int ct;
-  int nkb_next;
+struct PassCounter {
+  int ct, g, diag_left, pass_left, nkb, nkb_next;
   bool valid;
   template <typename NkbOf>
   __device__ void start(int ct0, int stride, int total, int s, NkbOf nkb_of) {
     ct = ct0;
     valid = ct < total;
-    q.start(s, valid ? nkb_of(ct) : 1);
+    nkb = valid ? nkb_of(ct) : 1;
     nkb_next = ct + stride < total ? nkb_of(ct + stride) : 1;
+    g = s - 1;
+    diag_left = s * nkb;
+    pass_left = diag_left < (int)PASS_BLOCKS ? diag_left : (int)PASS_BLOCKS;
   }
+  // the current k-block closes a pass
+  __device__ bool last() const { return pass_left == 1; }
+  // step to the next k-block; true when it begins a pass (of the next diagonal or tile)
   template <typename NkbOf>
-  __device__ void next(int stride, int total, int s, NkbOf nkb_of) {
-    q.next();
-    if (q.done()) {
-      ct += stride;
-      valid = ct < total;
-      if (valid) {
-        q.start(s, nkb_next);
-        nkb_next = ct + stride < total ? nkb_of(ct + stride) : 1;
+  __device__ bool next(int stride, int total, int s, NkbOf nkb_of) {
+    --diag_left;
+    if (--pass_left != 0) return false;
+    if (diag_left == 0) {
+      if (--g < 0) {
+        ct += stride;
+        valid = ct < total;
+        g = s - 1;
+        nkb = nkb_next;
+        nkb_next = valid && ct + stride < total ? nkb_of(ct + stride) : 1;
       }
+      diag_left = (g + 1) * nkb;
     }
+    pass_left = diag_left < (int)PASS_BLOCKS ? diag_left : (int)PASS_BLOCKS;
+    return true;
   }
 };
 
@@ -483,13 +496,13 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
       const uint32_t sa0 = smem_u32(smem);
       const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + A_BYTES);
       auto nkb_of = [&](int ct) { return GROUPED ? G.probs[G.items[ct].x].nkb : P.nkb; };
-      MmaCursor cur;
+      PassCounter cur;
       cur.start(blockIdx.x, gridDim.x, total_tiles, P.s, nkb_of);
       int stage = 0, buf = 0;
       uint32_t phase = 0, tph = 0;  // tph bit b: phase of accumulator b's full barrier
       uint64_t ad = ad0, bd = bd0;
       bool ok = cur.valid;
-      bool first = cur.q.pass_first(), last = cur.q.pass_last();
+      bool first = true, last = cur.last();
       if (ok) ok = mbar_wait(tempty0, 1, abort_flag, P.err);  // first pass: buffer 0 is free
       if (ok) ok = mbar_wait(full0, 0, abort_flag, P.err);
       tc_fence_after();
@@ -500,9 +513,8 @@ oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
         mma_f8(d_tmem, ad + 2, bd + 2, 1u);
         mma_f8(d_tmem, ad + 4, bd + 4, 1u);
         // ---- next k-block, while two MMAs are still queued
-        cur.next(gridDim.x, total_tiles, P.s, nkb_of);
-        const bool nvalid = cur.valid;
-        const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
+        const bool nfirst = cur.next(gridDim.x, total_tiles, P.s, nkb_of);
+        const bool nvalid = cur.valid, nlast = cur.last();
         const int nstage = stage + 1 == STAGES ? 0 : stage + 1;
         const uint32_t nphase = nstage == 0 ? phase ^ 1u : phase;
         const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
@@ -705,13 +717,13 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       const uint32_t sa0 = smem_u32(smem);
       const uint64_t ad0 = smem_desc(sa0), bd0 = smem_desc(sa0 + PAIR_A_BYTES);
       auto nkb_of = [&](int) { return P.nkb; };
-      MmaCursor cur;
+      PassCounter cur;
       cur.start(pair_id, num_pairs, total_tiles, P.s, nkb_of);
       int stage = 0, buf = 0;
       uint32_t phase = 0, tph = 0;
       uint64_t ad = ad0, bd = bd0;
       bool ok = cur.valid;
-      bool first = cur.q.pass_first(), last = cur.q.pass_last();
+      bool first = true, last = cur.last();
       if (ok) ok = mbar_wait_pair<true>(tempty0, 1, abort_flag, peer_abort, P.err);
       if (ok) ok = mbar_wait_pair<false>(full0, 0, abort_flag, peer_abort, P.err);
       tc_fence_after();
@@ -720,9 +732,8 @@ oz_gemm_tc_pair(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         mma_f8_pair(d_tmem, ad, bd, first ? 0u : 1u);
         mma_f8_pair(d_tmem, ad + 2, bd + 2, 1u);
         mma_f8_pair(d_tmem, ad + 4, bd + 4, 1u);
-        cur.next(num_pairs, total_tiles, P.s, nkb_of);
-        const bool nvalid = cur.valid;
-        const bool nfirst = cur.q.pass_first(), nlast = cur.q.pass_last();
+        const bool nfirst = cur.next(num_pairs, total_tiles, P.s, nkb_of);
+        const bool nvalid = cur.valid, nlast = cur.last();
         const int nstage = stage + 1 == NST ? 0 : stage + 1;
         const uint32_t nphase = nstage == 0 ? phase ^ 1u : phase;
         const uint64_t nad = nstage == 0 ? ad0 : ad + STAGE_STEP, nbd = nstage == 0 ? bd0 : bd + STAGE_STEP;
@@ -1067,17 +1078,18 @@ cudaError_t ozaki_gemm_tc(const OzakiSplit& A, const OzakiSplit& B, int64_t m, i
   // Engine form: CTA pairs issuing cta_group::2 MMAs on 256 x 256 tiles from two 128-row
   // tiles up (their operand traffic per SM is two thirds of the one-SM form's and a ring of
   // six 32 KB stages looks ahead 1.5x as far), else one CTA per SM on 128 x 256 tiles;
-  // TMM_TC_CLUSTER=1 or =pair forces a form.  Wave pacing (lag 2 chunks of 64 k-blocks) is
-  // on for the pair form, which drifts apart without it, and off for the one-SM form, which
-  // it slowed by 2-4 %.  Measured at m = n = 32768, k = 16384, 11 slices, under the power
-  // limit: one-SM 740 ms, pair 875 ms, pair with pacing 694 ms per launch; at m = n = 8192:
-  // 46.5, 43.4, 43.3 ms.
+  // TMM_TC_CLUSTER=1 or =pair forces a form.  Wave pacing is on for the pair form, which
+  // drifts apart without it, and off for the one-SM form, which it slowed by 2-4 %.  Measured
+  // at m = n = 32768, k = 16384, 11 slices, under the power limit: one-SM 740-754 ms, pair
+  // 871 ms, pair with a lag of 2 chunks of 64 k-blocks 700-714 ms, with a lag of 1 chunk
+  // 688-700 ms per launch (the tighter lag costs ~3 % more cycles per launch but draws less
+  // power, so the clock runs 5-9 % higher); at m = n = 8192: 46.5, 43.4, 43.3 ms.
   int cm = (m + tc::BM - 1) / tc::BM >= 2 ? 0 : 1;  // 0: pair
   if (const char* env = getenv("TMM_TC_CLUSTER")) {
     if (!strcmp(env, "pair")) cm = 0;
     else if (!strcmp(env, "1")) cm = 1;
   }
-  P.pace_lag = cm == 0 ? 2 : 0;
+  P.pace_lag = cm == 0 ? 1 : 0;
   P.pace_chunk = 64;
   P.pace_ns = 20000;
   if (const char* env = getenv("TMM_TC_PACE")) P.pace_lag = atoi(env) < 0 ? 0 : atoi(env);

@@ -4,6 +4,11 @@
 //   tcgen05 tcgen05.mma.cta_group::1.kind::f8f6f4, M128 N256 K32, e4m3 operands resident in shared
 //           (and kind::f16 with bf16 operands, M128 N256 K16, the FP32 engine's instruction)
 //           memory, issued back to back from one thread (tcgen05 Ozaki engine, pipe ceiling)
+//   pair    tcgen05.mma.cta_group::2.kind::f8f6f4, M256 N256 K32 on a cluster of two CTAs (the
+//           pair engine's instruction): back to back, with a commit to a stage barrier after
+//           every k-block, with that commit plus a probe of a completed barrier, with both
+//           plus a tcgen05.fence::after_thread_sync per k-block, and with all of that while a
+//           thread of another warp in each CTA spins on an mbarrier (as a waiting producer)
 // Every CTA runs a fixed number of iterations; the tcgen05 probe's one wait is bounded by %globaltimer.
 //
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -o engine_rates engine_rates.cu
@@ -176,6 +181,104 @@ __global__ void __launch_bounds__(128, 1) tcgen05_loop(int kblocks, int mode, lo
   }
 }
 
+// Cluster of two CTAs on one TPC; each stages 4 x (16 KB of A rows + 16 KB of its half of B)
+// filled with e4m3 1.0; the leader issues `kblocks` k-blocks of 4 cta_group::2 MMAs
+// (M256 N256 K32) into two alternating TMEM accumulators.
+// mode 0: back to back; mode 1: plus a commit of each k-block to a stage barrier in both CTAs
+// (multicast arrive, as the engine releases a stage); mode 2: mode 1 plus a probe of an
+// already-completed barrier between the third and fourth MMA; mode 3: mode 2 plus a
+// tcgen05.fence::after_thread_sync after each k-block's commit; mode 4: mode 3 while lane 0
+// of warp 1 in both CTAs polls the final barrier with try_wait until the MMAs are done.
+__global__ void __launch_bounds__(128, 1) tcgen05_pair_loop(int kblocks, int mode, long long* cycles, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t fin, done0, stage_bar[4];
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t rank;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+  for (int i = threadIdx.x; i < 4 * 32768 / 4; i += blockDim.x) ((uint32_t*)smem)[i] = 0x38383838u;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&fin)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done0)));
+    for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&stage_bar[i])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&done0)) : "memory");  // phase 0 done
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)), "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tslot;
+  constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+  const long long t0 = clock64();
+  if (warp == 0 && lane == 0 && rank == 0) {
+    const uint64_t ad0 = smem_desc(smem_u32(smem)), bd0 = smem_desc(smem_u32(smem + 16384));
+    uint64_t ad = ad0, bd = bd0;
+    const uint32_t d0 = smem_u32(&done0);
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const uint32_t d = tmem + (uint32_t)(((kb >> 9) & 1) * 256);
+      const uint32_t acc0 = (kb & 511) ? 1u : 0u;
+      asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+                   ::"r"(d), "l"(ad), "l"(bd), "r"(IDESC2), "r"(acc0));
+      asm volatile("tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 2), "l"(bd + 2), "r"(IDESC2));
+      asm volatile("tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 4), "l"(bd + 4), "r"(IDESC2));
+      const bool wrap = (kb & 3) == 3;
+      const uint64_t nad = wrap ? ad0 : ad + (32768 >> 4), nbd = wrap ? bd0 : bd + (32768 >> 4);
+      if (mode == 2 && !try_wait(d0, 0)) atomicOr(err, 2);
+      asm volatile("tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, 1;" ::"r"(d), "l"(ad + 6), "l"(bd + 6), "r"(IDESC2));
+      if (mode >= 1)
+        asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                     ::"r"(smem_u32(&stage_bar[kb & 3])), "h"((uint16_t)3) : "memory");
+      if (mode >= 3) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      ad = nad;
+      bd = nbd;
+    }
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(smem_u32(&fin)), "h"((uint16_t)3) : "memory");
+  }
+  if (mode == 4 && warp == 1 && lane == 0) {  // a spinning neighbour, bounded by %globaltimer
+    uint64_t g0, g1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+    while (!try_wait(smem_u32(&fin), 0)) {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+      if (g1 - g0 > 1000000000ull) {
+        atomicOr(err, 4);
+        break;
+      }
+    }
+  }
+  if (warp == 0 && lane == 0) {  // both CTAs: the leader's last commit arrives here too
+    uint64_t g0, g1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+    while (true) {
+      uint32_t ok;
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                   : "=r"(ok) : "r"(smem_u32(&fin)) : "memory");
+      if (ok) break;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+      if (g1 - g0 > 1000000000ull) {
+        atomicOr(err, 1);
+        break;
+      }
+    }
+    if (rank == 0) cycles[blockIdx.x >> 1] = clock64() - t0;
+  }
+  __syncwarp();
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
 static float time_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, a, b);
@@ -248,6 +351,52 @@ int main() {
              mode == 3 ? "tcgen05_f16_bf16_m128n256k16" : "tcgen05_f8f6f4_m128n256k32", form[mode],
              flop / time_ms(e0, e1) / 1e9, c / kblocks, 2.0 * 128 * 256 * kel * kblocks / c,
              2.0 * 128 * 256 * kel * kblocks / c * sms * (clk_khz * 1e3) / 1e12, herr);
+    }
+    CK(cudaFree(cyc));
+    CK(cudaFree(err));
+  }
+  for (int mode = 0; mode < 5; ++mode) {  // tcgen05 cta_group::2 e4m3 pipe on CTA pairs
+    const int kblocks = 20000, pairs = sms / 2;
+    const int smem = 4 * 32768 + 1024;
+    long long* cyc = nullptr;
+    int* err = nullptr;
+    CK(cudaMalloc(&cyc, pairs * sizeof(long long)));
+    CK(cudaMalloc(&err, sizeof(int)));
+    CK(cudaMemset(err, 0, sizeof(int)));
+    CK(cudaFuncSetAttribute(tcgen05_pair_loop, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(pairs * 2));
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(e0));
+      CK(cudaLaunchKernelEx(&cfg, tcgen05_pair_loop, kblocks, mode, cyc, err));
+      CK(cudaEventRecord(e1));
+      CK(cudaEventSynchronize(e1));
+      if (!rep) continue;
+      long long h[256];
+      int herr = 0;
+      const int n = pairs < 256 ? pairs : 256;
+      CK(cudaMemcpy(h, cyc, n * sizeof(long long), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+      double c = 0;
+      for (int i = 0; i < n; ++i) c += (double)h[i];
+      c /= n;
+      // per SM: a 128 x 256 half of the M256 tile, 128 e4m3 of K per k-block
+      const double flop_sm = 2.0 * 128 * 256 * 128;
+      static const char* form[5] = {"back_to_back", "commit_per_kblock", "commit_and_probe_per_kblock",
+                                    "commit_probe_and_fence_per_kblock", "same_with_a_spinning_neighbour_warp"};
+      printf("{\"probe\": \"tcgen05_pair_f8f6f4_m256n256k32\", \"issue_loop\": \"%s\", \"tflops\": %.1f, "
+             "\"cycles_per_kblock\": %.1f, \"flop_per_clk_per_sm\": %.0f, \"wait_error\": %d}\n",
+             form[mode], flop_sm * 2 * pairs * kblocks / time_ms(e0, e1) / 1e9, c / kblocks,
+             flop_sm * kblocks / c, herr);
     }
     CK(cudaFree(cyc));
     CK(cudaFree(err));
