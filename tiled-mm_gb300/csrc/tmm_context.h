@@ -135,6 +135,11 @@ struct tmm_context {
   tmm::GrowBuffer batch_f32_scratch;
   cudaStream_t batch_f32_stream = nullptr;
   cudaEvent_t batch_f32_fork = nullptr, batch_f32_join = nullptr;
+  // lanes of the batch's many small launches and copies (the FP32 problems' splits, the
+  // copies back of the problems outside the Ozaki pipeline): forked from and joined into the
+  // stream that would otherwise run them one after another
+  std::vector<cudaStream_t> batch_lanes;
+  std::vector<cudaEvent_t> batch_lane_events;  // [0]: fork, [1 + i]: lane i done
   bool f32_simt = false;  // TMM_F32_KERNEL=simt: the FFMA tile kernel instead
 
   // the size class of the last autotuned call (tmm_get_autotune_report)

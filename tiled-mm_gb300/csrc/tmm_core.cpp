@@ -425,6 +425,8 @@ extern "C" int tmm_destroy(tmm_context* ctx) {
   if (ctx->batch_f32_stream) cudaStreamDestroy(ctx->batch_f32_stream);
   if (ctx->batch_f32_fork) cudaEventDestroy(ctx->batch_f32_fork);
   if (ctx->batch_f32_join) cudaEventDestroy(ctx->batch_f32_join);
+  for (auto b : ctx->batch_lanes) cudaStreamDestroy(b);
+  for (auto e : ctx->batch_lane_events) cudaEventDestroy(e);
   for (auto& b : ctx->cz_scratch) b.release();
   for (auto& b : ctx->f32_scratch) b.release();
   for (auto b : ctx->oz_branches) cudaStreamDestroy(b);
@@ -1780,19 +1782,56 @@ int plan_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, 
   return TMM_SUCCESS;
 }
 
-// splits and the grouped launch on stream t (operands already in place)
+// Lanes: BATCH_LANES streams that fork from stream s (lanes_fork), take work round robin,
+// and join back into s (lanes_join).  Small kernels and copies queued on one stream run one
+// after another with the launch latency of each exposed (512 splits of a 512-problem batch:
+// ~10 ms; 256 copies back of its FP32 results: ~15 ms); spread over the lanes they overlap.
+constexpr int BATCH_LANES = 4;
+
+int ensure_batch_lanes(tmm_context* ctx) {
+  while (ctx->batch_lanes.size() < (size_t)BATCH_LANES) {
+    cudaStream_t ls;
+    TMM_CUDA(ctx, cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking));
+    ctx->batch_lanes.push_back(ls);
+  }
+  while (ctx->batch_lane_events.size() < 1 + (size_t)BATCH_LANES) {
+    cudaEvent_t ev;
+    TMM_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ctx->batch_lane_events.push_back(ev);
+  }
+  return TMM_SUCCESS;
+}
+
+int lanes_fork(tmm_context* ctx, cudaStream_t s) {
+  TMM_CUDA(ctx, cudaEventRecord(ctx->batch_lane_events[0], s));
+  for (int q = 0; q < BATCH_LANES; ++q) TMM_CUDA(ctx, cudaStreamWaitEvent(ctx->batch_lanes[(size_t)q], ctx->batch_lane_events[0], 0));
+  return TMM_SUCCESS;
+}
+
+int lanes_join(tmm_context* ctx, cudaStream_t s) {
+  for (int q = 0; q < BATCH_LANES; ++q) {
+    TMM_CUDA(ctx, cudaEventRecord(ctx->batch_lane_events[1 + (size_t)q], ctx->batch_lanes[(size_t)q]));
+    TMM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->batch_lane_events[1 + (size_t)q], 0));
+  }
+  return TMM_SUCCESS;
+}
+
+// splits (on the lanes) and the grouped launch on stream t (operands already in place)
 int enqueue_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const BatchF32Plan& P,
                       cudaStream_t t) {
   if (P.ids.empty()) return TMM_SUCCESS;
   char* base = (char*)ctx->batch_f32_scratch.ptr;
+  if (int st = lanes_fork(ctx, t)) return st;
   for (size_t j = 0; j < P.ids.size(); ++j) {
     const tmm::BatchProblem& d = dev[(size_t)P.ids[j]];
+    cudaStream_t ls = ctx->batch_lanes[j % BATCH_LANES];
     // lines of op(A): its rows (adjacent when A is not transposed); of op(B): its columns
-    cudaError_t e = tmm::f32tc_split_lines((const float*)d.a, d.lda, d.opa == tmm::OP_N, d.m, d.k, base + P.a_off[j], t);
+    cudaError_t e = tmm::f32tc_split_lines((const float*)d.a, d.lda, d.opa == tmm::OP_N, d.m, d.k, base + P.a_off[j], ls);
     if (e == cudaSuccess)
-      e = tmm::f32tc_split_lines((const float*)d.b, d.ldb, d.opb != tmm::OP_N, d.n, d.k, base + P.b_off[j], t);
+      e = tmm::f32tc_split_lines((const float*)d.b, d.ldb, d.opb != tmm::OP_N, d.n, d.k, base + P.b_off[j], ls);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batched FP32 split");
   }
+  if (int st = lanes_join(ctx, t)) return st;
   cudaError_t e = tmm::f32tc_gemm_grouped(base + P.arena_off, P.arena_bytes, base + P.image_off, P.n_probs, P.n_items,
                                           (int*)base, t);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched FP32 launch");
@@ -1842,8 +1881,11 @@ int enqueue_batch(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, c
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
   ctx->stats.kernels += (n_f64 > 0) + (n_work - n_f64 > 0) + (any_k0 ? 1 : 0);
   if ((st = fork_batch_f32(ctx, dev, f32, s, true))) return st;
-  for (int i = 0; i < count; ++i)
-    if (!on_branch[(size_t)i] && (st = copy_problem_out(ctx, host[i], dev[i], s))) return st;
+  if ((st = lanes_fork(ctx, s))) return st;
+  for (int i = 0, q = 0; i < count; ++i)
+    if (!on_branch[(size_t)i] && (st = copy_problem_out(ctx, host[i], dev[i], ctx->batch_lanes[(size_t)(q++ % BATCH_LANES)])))
+      return st;
+  if ((st = lanes_join(ctx, s))) return st;
   return join_batch_ozaki(ctx, oz, s, true);
 }
 
@@ -1960,6 +2002,7 @@ extern "C" int tmm_gemm_batched(tmm_context* ctx, int count, const tmm_batch_pro
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_f32_fork, cudaEventDisableTiming));
     TMM_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch_f32_join, cudaEventDisableTiming));
   }
+  if (int st0 = ensure_batch_lanes(ctx)) return st0;
   const int kernels = (n_f64 > 0) + (n_work - n_f64 > 0) + any_k0 + oz.kernels +
                       (f32.ids.empty() ? 0 : 2 * (int)f32.ids.size() + 1);
   const size_t pb_al = (pb.size() + 255) / 256 * 256;
