@@ -726,6 +726,8 @@ def run_batched(args, rank, world, dist, log, ozaki: bool = False) -> dict:
     err_probs = sorted(f64, key=lambda p: -p["m"] * p["n"] * p["k"])[:24]
 
     def f64_error():
+        if not err_probs:  # an FP32-only batch (--batch-dtypes f32) has no FP64 result to check
+            return float("nan")
         return max(tmm.error_metric(p["trans_a"], p["trans_b"], p["m"], p["n"], p["k"], 1.0, p["a"], p["ld_a"],
                                     p["b"], p["ld_b"], 0.0, None, p["m"], p["c"], p["ld_c"], n_samples=256, seed=5)
                    for p in err_probs)
@@ -753,6 +755,8 @@ def run_batched(args, rank, world, dist, log, ozaki: bool = False) -> dict:
         octx.set_ozaki_engine(args.engine)
         calib = {}
         slices = args.slices
+        if not slices and not err_probs:
+            slices = 11
         if not slices:
             for s_try in range(7, 14):
                 octx.set_path(tmm.PATH_OZAKI, s_try)
