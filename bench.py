@@ -56,7 +56,7 @@ TCGEN05_E4M3_FLOP_PER_CLK_SM = 16384.0
 # k = 16384, 11 slices: the same per-tile sequence, 2048 tiles instead of 32768); a launch of
 # another shape is scaled by its units (tiles x slice pairs x k-blocks), which assumes the
 # traffic per unit does not depend on the number of tiles.  None: no capture for this engine.
-ENGINE_DRAM_CAPTURE = {"launch_mnk": (8192, 8192, 16384), "slices": 11, "bytes": 179.23e9 + 11.28e9}
+ENGINE_DRAM_CAPTURE = {"launch_mnk": (8192, 8192, 16384), "slices": 11, "bytes": 125.42e9 + 11.26e9}
 
 WORKLOADS = {
     "ozaki32768": dict(m=32768, n=32768, k=32768, ta="N", tb="N", alpha=1.0, beta=0.0, kind=2, param=20.0,
