@@ -15,7 +15,6 @@
 // are ordered against compute with events only; each compute stream owns two
 // C tile slots, so the copy-back of one tile overlaps the next tile's k loop.
 #include <algorithm>
-#include <functional>
 #include <numeric>
 #include <chrono>
 #include <cmath>
@@ -1639,8 +1638,7 @@ int copy_problem_out(tmm_context* ctx, const tmm_batch_problem& h, const tmm::Ba
 // with host operands (host != nullptr) copies in, splits and products, copies out;
 // join_batch_ozaki makes s wait for the pipeline.
 int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, const BatchOzPlan& plan,
-                        cudaStream_t s, const tmm_batch_problem* host,
-                        const std::function<int(cudaStream_t)>* lead_copies = nullptr) {
+                        cudaStream_t s, const tmm_batch_problem* host) {
   if (plan.ids.empty()) return TMM_SUCCESS;
   cudaStream_t cin = ctx->oz_branches[1], comp = ctx->oz_branches[0], cout = ctx->oz_branches[2];
   const size_t nch = plan.chunks.size();
@@ -1654,9 +1652,6 @@ int enqueue_batch_ozaki(tmm_context* ctx, const std::vector<tmm::BatchProblem>& 
     TMM_CUDA(ctx, cudaStreamWaitEvent(cin, ctx->oz_fork, 0));
     TMM_CUDA(ctx, cudaStreamWaitEvent(cout, ctx->oz_fork, 0));
   }
-  // other copies that lead the chunks' on the copy stream (the batch's FP32 problems)
-  if (host && lead_copies)
-    if (int st = (*lead_copies)(cin)) return st;
   char* scratch = (char*)ctx->batch_oz_scratch.ptr;
   double* work = (double*)(scratch + plan.work_off);
   size_t li = 0;
@@ -1865,66 +1860,32 @@ int enqueue_batch(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, c
   const size_t rec = tmm::batch_problem_record_bytes();
   const void* dprobs = ctx->batch_meta.ptr;
   const void* dwork = (const char*)ctx->batch_meta.ptr + (rec * (size_t)count + 255) / 256 * 256;
-  std::vector<char> on_branch((size_t)count, 0), on_f32((size_t)count, 0);
+  std::vector<char> on_branch((size_t)count, 0);
   for (int id : oz.ids) on_branch[(size_t)id] = 1;
-  // Beside an Ozaki pipeline the FP32-engine problems lead: their copies go first on the
-  // pipeline's copy stream, their splits and grouped launch run on the FP32 stream as soon as
-  // those copies have landed, and their results go back on the lanes while the chunks' operands
-  // still come in (the other direction of the link); only the chunks' own work trails the last
-  // copy in.  (Queued after the chunks instead, that work is a tail of its own after the last
-  // copy in.)
-  const bool f32_lead = !oz.ids.empty() && !f32.ids.empty();
-  if (f32_lead)
-    for (int id : f32.ids) on_f32[(size_t)id] = 1;
-  std::function<int(cudaStream_t)> lead = [&](cudaStream_t cin) -> int {
-    for (int id : f32.ids)
-      if (int st1 = copy_problem_in(ctx, host[id], dev[(size_t)id], cin)) return st1;
-    TMM_CUDA(ctx, cudaEventRecord(ctx->batch_f32_fork, cin));
-    return TMM_SUCCESS;
-  };
-  int st = enqueue_batch_ozaki(ctx, dev, oz, s, host, f32_lead ? &lead : nullptr);
+  // the Ozaki pipeline first: it moves its own operands; the other problems' operands follow
+  // its chunks on the same copy stream, so that the engine's chunks are not kept waiting
+  int st = enqueue_batch_ozaki(ctx, dev, oz, s, host);
   if (st) return st;
-  cudaStream_t t = ctx->batch_f32_stream;
-  if (f32_lead) {
-    TMM_CUDA(ctx, cudaStreamWaitEvent(t, ctx->batch_f32_fork, 0));
-    if ((st = enqueue_batch_f32(ctx, dev, f32, t))) return st;
-    if ((st = lanes_fork(ctx, t))) return st;
-    int q = 0;
-    for (int id : f32.ids)
-      if ((st = copy_problem_out(ctx, host[id], dev[(size_t)id], ctx->batch_lanes[(size_t)(q++ % BATCH_LANES)])))
-        return st;
-    if ((st = lanes_join(ctx, t))) return st;
-  }
-  // the other problems' operands follow the Ozaki chunks on the same copy stream, so that the
-  // engine's chunks are not kept waiting
   const bool after_oz = !oz.ids.empty();
   cudaStream_t cs = after_oz ? ctx->oz_branches[1] : s;
   for (int i = 0; i < count; ++i)
-    if (!on_branch[(size_t)i] && !on_f32[(size_t)i] && (st = copy_problem_in(ctx, host[i], dev[i], cs))) return st;
+    if (!on_branch[(size_t)i] && (st = copy_problem_in(ctx, host[i], dev[i], cs))) return st;
   if (after_oz) {
     cudaEvent_t ev = ctx->oz_branch_done[2 * (size_t)BATCH_OZ_CHUNKS + 3 + (size_t)BATCH_OZ_SPLIT_STREAMS];
     TMM_CUDA(ctx, cudaEventRecord(ev, cs));
     TMM_CUDA(ctx, cudaStreamWaitEvent(s, ev, 0));
   }
-  if (!f32_lead && (st = fork_batch_f32(ctx, dev, f32, s, false))) return st;
+  if ((st = fork_batch_f32(ctx, dev, f32, s, false))) return st;
   cudaError_t e = tmm::batch_launch(dprobs, count, dwork, n_f64, n_work - n_f64, any_k0, s, ctx->batch_aux,
                                     ctx->batch_fork, ctx->batch_join);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched kernel launch");
   ctx->stats.kernels += (n_f64 > 0) + (n_work - n_f64 > 0) + (any_k0 ? 1 : 0);
-  if (f32_lead) {
-    for (int i = 0; i < count; ++i)
-      if (!on_branch[(size_t)i] && !on_f32[(size_t)i] && (st = copy_problem_out(ctx, host[i], dev[i], s))) return st;
-    TMM_CUDA(ctx, cudaEventRecord(ctx->batch_f32_join, t));
-    TMM_CUDA(ctx, cudaStreamWaitEvent(s, ctx->batch_f32_join, 0));
-  } else {
-    if ((st = fork_batch_f32(ctx, dev, f32, s, true))) return st;
-    if ((st = lanes_fork(ctx, s))) return st;
-    for (int i = 0, q = 0; i < count; ++i)
-      if (!on_branch[(size_t)i] &&
-          (st = copy_problem_out(ctx, host[i], dev[i], ctx->batch_lanes[(size_t)(q++ % BATCH_LANES)])))
-        return st;
-    if ((st = lanes_join(ctx, s))) return st;
-  }
+  if ((st = fork_batch_f32(ctx, dev, f32, s, true))) return st;
+  if ((st = lanes_fork(ctx, s))) return st;
+  for (int i = 0, q = 0; i < count; ++i)
+    if (!on_branch[(size_t)i] && (st = copy_problem_out(ctx, host[i], dev[i], ctx->batch_lanes[(size_t)(q++ % BATCH_LANES)])))
+      return st;
+  if ((st = lanes_join(ctx, s))) return st;
   return join_batch_ozaki(ctx, oz, s, true);
 }
 
