@@ -48,8 +48,12 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 # (tiled-mm_gb300/peaks/cublaslt_e4m3.py, 8192^3).  The tcgen05 pipe retires 16384 e4m3 FLOP per
 # clock and SM (512 cycles per 128 x 256 x 128 k-block): the tensor roofline of the slice-product
 # kernel is that rate at the SM clock measured during the timed region.
+# tcgen05_e4m3_sustained_digits_tflops: the CTA-pair instruction back to back on digit operands
+# for about a second, at the power limit (512 cycles per k-block at ~1.71 GHz), the ceiling of
+# a kernel that keeps the pipe busy for a whole long launch
 MEASURED_ENGINE_PEAKS = {"imma_s8_tops": 157.9, "dmma_f64_tflops": 1.099,
-                         "tcgen05_e4m3_tflops": 4847.2, "cublaslt_e4m3_tflops": 3948.0}
+                         "tcgen05_e4m3_tflops": 4847.2, "cublaslt_e4m3_tflops": 3948.0,
+                         "tcgen05_e4m3_sustained_digits_tflops": 4262.0}
 TCGEN05_E4M3_FLOP_PER_CLK_SM = 16384.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one slice-product launch, from one
 # ncu capture of a smaller launch with the headline's k tile and slice count (m = n = 8192,
@@ -649,6 +653,8 @@ def run_ours(args, w, rank, world, dist, log) -> dict:
             bf16 = measured_peaks().get("bf16_tflops") or 1910.1
             result["roofline"]["frac_of_other_ceilings"] = {
                 "cublaslt_e4m3_gemm": achieved / MEASURED_ENGINE_PEAKS["cublaslt_e4m3_tflops"],
+                "tcgen05_pipe_sustained_at_power_limit":
+                    achieved / MEASURED_ENGINE_PEAKS["tcgen05_e4m3_sustained_digits_tflops"],
                 "two_x_bf16_burst": achieved / (2.0 * bf16),
                 "tcgen05_pipe_at_max_clock": achieved / pipe_peak({"sm_mhz": max_mhz})[0]}
             # spec roofline of the host-pointer call: the slower of the slice products at the

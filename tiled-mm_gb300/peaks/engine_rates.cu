@@ -15,7 +15,10 @@
 //           each stage's release and re-arms its full barrier; the issuer probes the next
 //           stage's full barrier before the fourth MMA and waits on it when the probe fails),
 //           and variants of that handshake (producer parked instead of polling; issuer waiting
-//           after the fourth MMA instead of probing; 4 stages; other warps parked on a barrier)
+//           after the fourth MMA instead of probing; 4 stages; other warps parked on a barrier);
+//           finally back to back and with the engine's issue block for about a second each on
+//           digit operands (sustained load at the power limit), with the SM clock the cycle
+//           count and the event time imply
 // Every CTA runs a fixed number of iterations; the tcgen05 probe's one wait is bounded by %globaltimer.
 //
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 -o engine_rates engine_rates.cu
@@ -540,10 +543,11 @@ int main() {
     CK(cudaFree(cyc));
     CK(cudaFree(err));
   }
-  for (int run = 0; run < 15; ++run) {  // tcgen05 cta_group::2 e4m3 pipe on CTA pairs
-    const int mode = run < 5 ? run : (run < 7 ? 0 : (run < 9 ? 5 : run - 3));
-    const int fill = run < 5 ? 0 : (run < 7 ? run - 4 : (run < 9 ? run - 7 : 0));
-    const int kblocks = 20000, pairs = sms / 2;
+  for (int run = 0; run < 17; ++run) {  // tcgen05 cta_group::2 e4m3 pipe on CTA pairs
+    const int mode = run < 5 ? run : (run < 7 ? 0 : (run < 9 ? 5 : (run < 15 ? run - 3 : (run == 15 ? 0 : 11))));
+    const int fill = run < 5 ? 0 : (run < 7 ? run - 4 : (run < 9 ? run - 7 : (run < 15 ? 0 : 1)));
+    const bool sustained = run >= 15;
+    const int kblocks = sustained ? 3000000 : 20000, pairs = sms / 2;
     const int smem = 6 * 32768 + 1024;
     long long* cyc = nullptr;
     int* err = nullptr;
@@ -586,10 +590,10 @@ int main() {
                                      "handshake_test_wait_probe_read_after_4th_mma"};
       static const char* fills[3] = {"e4m3_one", "ozaki_digits", "random_finite_e4m3"};
       printf("{\"probe\": \"tcgen05_pair_f8f6f4_m256n256k32\", \"issue_loop\": \"%s\", \"operands\": \"%s\", "
-             "\"tflops\": %.1f, \"cycles_per_kblock\": %.1f, \"flop_per_clk_per_sm\": %.0f, \"wait_error\": %d, "
-             "\"failed_probes\": %d}\n",
-             form[mode], fills[fill], flop_sm * 2 * pairs * kblocks / time_ms(e0, e1) / 1e9, c / kblocks,
-             flop_sm * kblocks / c, herr[0], herr[1]);
+             "\"kblocks\": %d, \"ms\": %.1f, \"tflops\": %.1f, \"cycles_per_kblock\": %.1f, "
+             "\"flop_per_clk_per_sm\": %.0f, \"implied_sm_mhz\": %.0f, \"wait_error\": %d, \"failed_probes\": %d}\n",
+             form[mode], fills[fill], kblocks, time_ms(e0, e1), flop_sm * 2 * pairs * kblocks / time_ms(e0, e1) / 1e9,
+             c / kblocks, flop_sm * kblocks / c, c / (time_ms(e0, e1) * 1e3), herr[0], herr[1]);
     }
     CK(cudaFree(cyc));
     CK(cudaFree(err));
