@@ -1784,8 +1784,9 @@ int plan_batch_f32(tmm_context* ctx, const std::vector<tmm::BatchProblem>& dev, 
 
 // Lanes: BATCH_LANES streams that fork from stream s (lanes_fork), take work round robin,
 // and join back into s (lanes_join).  Small kernels and copies queued on one stream run one
-// after another with the launch latency of each exposed (512 splits of a 512-problem batch:
-// ~10 ms; 256 copies back of its FP32 results: ~15 ms); spread over the lanes they overlap.
+// after another, each after the previous one's launch latency; spread over the lanes their
+// latencies overlap (the 512 FP32 splits and 256 copies back of a 512-problem batch: 57.7
+// against 58.5 ms per call).
 constexpr int BATCH_LANES = 4;
 
 int ensure_batch_lanes(tmm_context* ctx) {
